@@ -1,0 +1,372 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 qsl backend: gates/s and HBM GB/s at 30 qubits, FP64.
+
+Workload: the plain Default-backend path on a 30-qubit complex128 state
+(16 GiB), a seeded layered random circuit of depth 40: per layer one gate
+per qubit from {hadamard, rotateX, rotateY, rotateZ, phase} (angles
+U[0, 2pi)) and 15 two-qubit gates (controlNot or controlPhase, random
+control/target over all qubits).  One step is one layer (45 gates); the
+state carries over from step to step, so K = 40 steps is the whole circuit.
+After the timed layers the benchmark measures 8 random qubits and draws a
+100,000-shot sampleAll, each timed on its own and reported in `config`.
+
+value        gates/s over the K timed layers, state resident in HBM, timed with
+             CUDA events on the state's stream (max over ranks).
+roofline     the kernel with the largest share of the timed gate time: its
+             algorithmic bytes per launch (2 x 16 B x amplitudes the
+             reference's loop changes) over its mean launch time, against the
+             measured HBM copy bandwidth (MEASURED_PEAKS.json).
+e2e          the same metric through the C ABI from pinned host memory: the
+             state uploaded with qslc_set_state, K layers, the 8 measurements
+             and the sampleAll outcomes read back, all inside the timed region.
+cpu_baseline the oracle (a C restatement of the reference's OpenMP backend)
+             on the host cores, on a bounded sample of the same circuit.
+
+`--impl reference` times that CPU implementation alone (the reference
+cannot be built on the GPU machine), with every host thread, on the same
+config and metric; its step is a bounded sample of a layer (see --ref-gates).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from qsl_gb300 import workloads  # noqa: E402
+
+N_QUBITS = 30
+LAYERS = 40
+SEED = 20240601
+METRIC = "gates/s & HBM GB/s at 30q FP64"
+UNIT = "gates/s"
+
+
+def layers_of(circ, n):
+    per = n + n // 2
+    return [circ[i:i + per] for i in range(0, len(circ), per)]
+
+
+def alg_bytes(gate: str, n: int) -> int:
+    """Bytes the reference's loop reads and writes for one gate on n qubits
+    (complex128): 2 x 16 B x amplitudes it changes."""
+    amps = {
+        "hadamard": 1 << n, "rotateX": 1 << n, "rotateY": 1 << n, "rotateZ": 1 << n,
+        "pauliX": 1 << n, "pauliY": 1 << n,
+        "phase": 1 << (n - 1), "pauliZ": 1 << (n - 1),
+        "controlNot": 1 << (n - 1), "controlPhase": 1 << (n - 2), "controlZ": 1 << (n - 2),
+    }[gate]
+    return 2 * 16 * amps
+
+
+def kernel_of(gate: str) -> str:
+    return {"hadamard": "k_pair1<H>", "rotateX": "k_pair1<RX>", "rotateY": "k_pair1<RY>",
+            "rotateZ": "k_pair1<RZ>", "phase": "k_diag1<PHASE>", "controlNot": "k_pair2<SWAP>",
+            "controlPhase": "k_diag2<PHASE>"}[gate]
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_sample(circ, n, seconds=20.0, threads=None):
+    """Time the oracle's OpenMP restatement of the reference on the host
+    cores: the circuit's gates in order on a fresh n-qubit state, until
+    `seconds` have passed (at least 2 gates).  Returns (gates/s, gates, threads)."""
+    import oracle
+    oracle.build(reference=False)
+    threads = threads or os.cpu_count() or 1
+    sim = oracle.PortQubits(n, nthreads=threads)
+    sim.gate("rotateX", 0, None, 0.1)          # first touch of the host state
+    done, t0 = 0, time.perf_counter()
+    for g in circ:
+        sim.gate(*g)
+        done += 1
+        if done >= 2 and time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    return done / dt, done, threads
+
+
+def run_gpu(args):
+    import torch
+    import qsl_gb300 as q
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    n = args.qubits
+    circ = workloads.layered_mixed(n, LAYERS, SEED + rank)
+    layers = layers_of(circ, n)
+    stream = torch.cuda.Stream()
+    sim = q.Qubits(n)
+    sim.set_stream(stream.cuda_stream)
+
+    def run_layer(li, timing):
+        for g, a, b, x in layers[li % len(layers)]:
+            if timing is not None:
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            sim.gate(g, a, b, x)
+            if timing is not None:
+                e1.record(stream)
+                timing.append((g, e0, e1))
+
+    # warm-up layers (the circuit's own first layers)
+    for w in range(args.warmup):
+        run_layer(w, None)
+    sim.synchronize()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+
+    clocks = ClockSampler()
+    clocks.start()
+    timing = []
+    launches0 = sim.launches()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t_start.record(stream)
+    for k in range(args.steps):
+        run_layer(args.warmup + k, timing)
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    launches = sim.launches() - launches0
+    clk = clocks.stop()
+    total_ms = t_start.elapsed_time(t_end)
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ngates = sum(len(layers[(args.warmup + k) % len(layers)]) for k in range(args.steps))
+
+    # per-kernel breakdown from the per-gate events
+    per = {}
+    for g, e0, e1 in timing:
+        ms = e0.elapsed_time(e1)
+        d = per.setdefault(kernel_of(g), {"launches": 0, "ms": 0.0, "bytes": 0})
+        d["launches"] += 1
+        d["ms"] += ms
+        d["bytes"] += alg_bytes(g, n)
+    gate_ms = sum(d["ms"] for d in per.values())
+    top_name, top = max(per.items(), key=lambda kv: kv[1]["ms"])
+    peak, peak_kind = peaks()
+    achieved = top["bytes"] / top["launches"] / (top["ms"] / top["launches"] * 1e-3) / 1e9
+    all_gbs = sum(d["bytes"] for d in per.values()) / (gate_ms * 1e-3) / 1e9
+
+    # measurement and sampling on the evolved state
+    rng = np.random.default_rng(SEED)
+    mq = [int(x) for x in rng.choice(n, 8, replace=False)]
+    mu = workloads.uniforms(8, SEED + 1)
+    su = workloads.uniforms(args.shots, SEED + 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    outs = [sim.measure(a, float(u)) for a, u in zip(mq, mu)]
+    t1 = time.perf_counter()
+    shots = sim.sample_shots(su)
+    t2 = time.perf_counter()
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        host = torch.empty((1 << n) * 2, dtype=torch.float64, pin_memory=True)
+        hv = host.numpy().view(np.complex128)
+        hv[:] = 0
+        hv[0] = 1
+        sim2 = q.Qubits(n)
+        sim2.set_stream(stream.cuda_stream)
+        torch.cuda.synchronize()
+        e0 = time.perf_counter()
+        sim2.L.qslc_set_state(sim2.h, hv.ctypes.data, hv.size)
+        for k in range(args.steps):
+            for g, a, b, x in layers[k % len(layers)]:
+                sim2.gate(g, a, b, x)
+        o2 = [sim2.measure(a, float(u)) for a, u in zip(mq, mu)]
+        sh2 = sim2.sample_shots(su)
+        e1 = time.perf_counter()
+        g2 = sum(len(layers[k % len(layers)]) for k in range(args.steps))
+        e2e = {"value": g2 / (e1 - e0), "unit": UNIT,
+               "h2d_bytes_per_step": int(hv.nbytes / args.steps),
+               "d2h_bytes_per_step": int((sh2.nbytes + 8 * len(o2)) / args.steps),
+               "includes": "qslc_set_state of the 16 GiB state from pinned host memory, K layers, "
+                           "8 measurements, 100k-shot sampleAll read back"}
+        del sim2, host
+
+    line = {
+        "metric": METRIC, "value": ngates / (total_ms * 1e-3) * world, "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {
+            "workload": f"plain FP64 {n}-qubit layered random circuit (depth {LAYERS}): per layer "
+                        f"{n} one-qubit gates + {n // 2} controlNot/controlPhase; one layer per step",
+            "nqubits": n, "state_bytes": (1 << n) * 16, "gates_timed": ngates,
+            "parallelism": "replicas" if world > 1 else "single GPU",
+            "l2": "state (16 GiB) is larger than L2 (129 MB); no flush needed",
+            "hbm_gbs_all_gates": all_gbs,
+            "measure8_ms": (t1 - t0) * 1e3, "measure_outcomes": outs,
+            "sample_shots": args.shots, "sample_ms": (t2 - t1) * 1e3,
+            "kernels": {k: {"launches": v["launches"], "ms": v["ms"],
+                            "gbs": v["bytes"] / (v["ms"] * 1e-3) / 1e9,
+                            "share": v["ms"] / gate_ms} for k, v in per.items()},
+        },
+        "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": args.traffic},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    if e2e:
+        line["e2e"] = e2e
+    if rank == 0 and not args.no_cpu:
+        v, done, thr = cpu_sample(circ, n, seconds=args.cpu_seconds)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": thr, "kind": "port",
+                                "sample": f"first {done} gates of the same {n}-qubit circuit, "
+                                          f"OpenMP restatement of the reference's Omp backend"}
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_reference(args):
+    """The reference's CPU algorithm (its C restatement: the reference itself
+    does not build on the GPU machine) on every host thread."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+    oracle.build(reference=False)
+    n = args.qubits
+    circ = workloads.layered_mixed(n, LAYERS, SEED)
+    layers = layers_of(circ, n)
+    threads = os.cpu_count() or 1
+    sim = oracle.PortQubits(n, nthreads=threads)
+    sim.gate("rotateX", 0, None, 0.1)
+    per_step = max(1, args.ref_gates)
+    k = 0
+
+    def step(li):
+        for g in layers[li % len(layers)][:per_step]:
+            sim.gate(*g)
+
+    for w in range(args.warmup):
+        step(w)
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        step(args.warmup + s)
+        k += min(per_step, len(layers[(args.warmup + s) % len(layers)]))
+    dt = time.perf_counter() - t0
+    v = k / dt
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"plain FP64 {n}-qubit layered random circuit (depth {LAYERS}), "
+                               f"the first {per_step} gates of each layer per step",
+                   "nqubits": n},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{k} gates: the first {per_step} gates of {args.steps} layers"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=LAYERS)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--qubits", type=int, default=N_QUBITS)
+    ap.add_argument("--shots", type=int, default=100_000)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-gates", type=int, default=2)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="dram bytes per launch of the top kernel from an ncu capture")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,192 @@
+/*
+ * qslc.h -- C ABI of the GB300 state-vector backend for qsl.
+ *
+ * The reference library (lanamineh/qsl) exposes its simulators only as the
+ * C++ class template qsl::Qubits<Type, Fp>; it has no C or foreign-function
+ * interface.  These entry points are the narrowest boundary that carries
+ * that member API across a shared-library edge: an opaque handle, plain
+ * pointers and sizes, and an int status.  include/qsl/qubits/cuda.hpp
+ * rebuilds qsl::Qubits on top of them, and any FFI (ctypes, cgo, JNI) can
+ * bind them directly.  Each declaration names the qsl member it stands for
+ * (file:line inside the qsl project).
+ *
+ * Numerics: amplitudes, probabilities and sampled outcomes are the bits the
+ * reference's Default backend produces on the same inputs (every product
+ * and sum is rounded on its own, Hadamard divides by sqrt(2), sums run in
+ * the reference's order), given the same uniforms for measurement.
+ *
+ * Threading: one handle is one CUDA stream.  Gate calls are asynchronous;
+ * calls that return host values synchronise that stream.  A handle must not
+ * be used from two threads at once (qsl's objects are not thread-safe
+ * either).
+ */
+#ifndef QSLC_H
+#define QSLC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define QSLC_API __attribute__((visibility("default")))
+#else
+#define QSLC_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct qslc_state qslc_state;
+
+/* status codes */
+enum {
+    QSLC_OK = 0,
+    QSLC_EINVAL = 1,   /* bad argument: qubit index, size, gate code, weight */
+    QSLC_EOOM = 2,     /* device allocation failed */
+    QSLC_ECUDA = 3,    /* CUDA runtime error (message in qslc_last_error) */
+    QSLC_ETIMEOUT = 4, /* a bounded device-side wait gave up */
+    QSLC_ENOTNP = 5,   /* state is not number preserving (quantum.cpp:133-156) */
+    QSLC_ESIZE = 6     /* state size mismatch (default.cpp:70-74, :98-102) */
+};
+
+/* amplitude types: qsl::complex<double> and qsl::complex<float> */
+enum { QSLC_C128 = 0, QSLC_C64 = 1 };
+
+/* gate codes; names follow the qsl::Qubits members */
+enum {
+    /* one-qubit gates, qslc_gate1 (default.hpp:208-333) */
+    QSLC_PAULI_X = 0,
+    QSLC_PAULI_Y = 1,
+    QSLC_PAULI_Z = 2,
+    QSLC_HADAMARD = 3,
+    QSLC_PHASE = 4,
+    QSLC_ROTATE_X = 5,
+    QSLC_ROTATE_Y = 6,
+    QSLC_ROTATE_Z = 7,
+    /* two-qubit gates, qslc_gate2 (default.hpp:354-608); for the control*
+     * gates q1 is the control and q2 the target */
+    QSLC_CONTROL_NOT = 16,
+    QSLC_CONTROL_Y = 17,
+    QSLC_CONTROL_Z = 18,
+    QSLC_CONTROL_ROTATE_X = 19,
+    QSLC_CONTROL_ROTATE_Y = 20,
+    QSLC_CONTROL_ROTATE_Z = 21,
+    QSLC_CONTROL_PHASE = 22,
+    QSLC_CONTROL_HADAMARD = 23,
+    QSLC_SWAP = 24,
+    QSLC_FSWAP = 25,
+    QSLC_NP_ROTATE_X = 26,
+    QSLC_NP_ROTATE_Y = 27,
+    QSLC_NP_HADAMARD = 28
+};
+
+/* Library version, e.g. 100 for 0.1.0. */
+QSLC_API int qslc_version(void);
+
+/* Message of the last failed call on this thread ("" if none). */
+QSLC_API const char *qslc_last_error(void);
+
+/* Qubits(unsigned nqubits): the all-zero state |0...0>
+ * (default.cpp:39-46).  dtype is QSLC_C128 or QSLC_C64. */
+QSLC_API int qslc_create(unsigned nqubits, int dtype, qslc_state **out);
+
+/* NP Qubits(unsigned nqubits, unsigned nones): the basis state with the
+ * nones lowest bits set (np.cpp:42-55, :69-79).  EINVAL unless
+ * 1 <= nones < nqubits, as the reference throws.  Only the C(n, nones)
+ * amplitudes of that weight are stored on the device. */
+QSLC_API int qslc_create_np(unsigned nqubits, unsigned nones, int dtype, qslc_state **out);
+
+/* ~Qubits */
+QSLC_API int qslc_destroy(qslc_state *s);
+
+/* Qubits(const Qubits&) (default.hpp:137): a deep device-to-device copy. */
+QSLC_API int qslc_clone(const qslc_state *src, qslc_state **out);
+
+/* operator=(const Qubits&) (default.cpp:94-105): copies the amplitudes;
+ * QSLC_ESIZE when the qubit counts differ (the reference throws). */
+QSLC_API int qslc_assign(qslc_state *dst, const qslc_state *src);
+
+/* getNumQubits (default.cpp:114-118) */
+QSLC_API unsigned qslc_num_qubits(const qslc_state *s);
+
+/* 1 for a number-preserving state */
+QSLC_API int qslc_is_np(const qslc_state *s);
+
+/* QSLC_C128 or QSLC_C64 */
+QSLC_API int qslc_dtype(const qslc_state *s);
+
+/* Amplitudes held on the device: 2^n, or C(n, w) for an NP state. */
+QSLC_API uint64_t qslc_num_stored(const qslc_state *s);
+
+/* NP getNumOnes / setNumOnes (np.cpp:148-165); setNumOnes re-initialises
+ * to the lowest basis state of the new weight. */
+QSLC_API int qslc_num_ones(const qslc_state *s, unsigned *out);
+QSLC_API int qslc_set_num_ones(qslc_state *s, unsigned nones);
+
+/* reset (default.cpp:57-65; np.cpp:69-79) */
+QSLC_API int qslc_reset(qslc_state *s);
+
+/* setState (default.cpp:67-78; np.cpp:81-98).  `amps` points to n_amps
+ * host amplitudes of the handle's type; QSLC_ESIZE unless n_amps == 2^n.
+ * An NP state takes its new weight from the input, and QSLC_ENOTNP when
+ * the nonzero amplitudes have different weights. */
+QSLC_API int qslc_set_state(qslc_state *s, const void *amps, uint64_t n_amps);
+
+/* getState (default.cpp:108-112): writes all 2^n amplitudes to `amps`. */
+QSLC_API int qslc_get_state(const qslc_state *s, void *amps, uint64_t n_amps);
+
+/* setBasisState (default.cpp:80-90; np.cpp:100-116) */
+QSLC_API int qslc_set_basis(qslc_state *s, uint64_t index);
+
+/* One-qubit gate: pauliX, ..., rotateZ (gates.cpp:32-209; np/gates.cpp:33-113).
+ * `angle` is ignored by the gates without one. */
+QSLC_API int qslc_gate1(qslc_state *s, int gate, unsigned targ, double angle);
+
+/* Two-qubit gate (gates.cpp:215-682; np/gates.cpp:118-415).  EINVAL when
+ * q1 == q2 or either index is out of range. */
+QSLC_API int qslc_gate2(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle);
+
+/* prob(targ, outcome) (measure.cpp:126-147; np/measure.cpp:141-168).  The
+ * result is the reference's sequential sum, bit for bit; a complex64 state
+ * returns its float value widened to double. */
+QSLC_API int qslc_prob(qslc_state *s, unsigned targ, unsigned outcome, double *out);
+
+/* The collapse step of measure/postselect (measure.cpp:31-57;
+ * np/measure.cpp:32-70): scale the `outcome` half by `factor`, zero the
+ * other half. */
+QSLC_API int qslc_collapse(qslc_state *s, unsigned targ, unsigned outcome, double factor);
+
+/* measure(targ) (measure.cpp:81-107) with the uniform `u` that
+ * random.getNum() would return (:91). */
+QSLC_API int qslc_measure(qslc_state *s, unsigned targ, double u, int *outcome);
+
+/* postselect(targ, outcome) (measure.cpp:149-161); returns the probability. */
+QSLC_API int qslc_postselect(qslc_state *s, unsigned targ, unsigned outcome, double *prob);
+
+/* sample(targ, nsamples) (measure.cpp:191-216): counts[0], counts[1] for
+ * the nshots uniforms u[0..nshots). */
+QSLC_API int qslc_sample(qslc_state *s, unsigned targ, const double *u, uint64_t nshots,
+                uint64_t counts[2]);
+
+/* sampleAll(nsamples) (measure.cpp:220-234; np/measure.cpp:243-256): the
+ * basis index drawn by each uniform, in order, into out[0..nshots).  The
+ * reference folds these into a std::map of counts. */
+QSLC_API int qslc_sample_all(qslc_state *s, const double *u, uint64_t nshots, uint64_t *out);
+
+/* measureAll (measure.cpp:110-123): draw one index with `u`, then collapse
+ * to that basis state. */
+QSLC_API int qslc_measure_all(qslc_state *s, double u, uint64_t *outcome);
+
+/* Stream control.  `stream` is a cudaStream_t; NULL selects the handle's
+ * own stream. */
+QSLC_API int qslc_set_stream(qslc_state *s, void *stream);
+QSLC_API void *qslc_get_stream(const qslc_state *s);
+QSLC_API int qslc_synchronize(qslc_state *s);
+
+/* Kernels launched through this handle since it was created. */
+QSLC_API uint64_t qslc_launch_count(const qslc_state *s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QSLC_H */

@@ -1,0 +1,306 @@
+"""qsl_gb300 -- a GB300 (sm_103a) state-vector backend for qsl.
+
+The product is the shared library ``libqslc.so`` built from ``csrc/`` and
+its C ABI (``include/qslc.h``); C++ users get ``qsl::Qubits<qsl::Type::Cuda,
+Fp>`` from ``include/qsl/qubits/cuda.hpp``.  This module binds the same C
+ABI with ctypes and mirrors the reference's member API (``pauliX``,
+``rotateX``, ``controlNot``, ``prob``, ``measure``, ``sampleAll``, ...) for
+Python callers, tests and the benchmark.
+
+There is no CPU fallback: if ``libqslc.so`` is missing, or CUDA reports no
+device, constructing a state raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libqslc.so")
+
+C128, C64 = 0, 1
+OK, EINVAL, EOOM, ECUDA, ETIMEOUT, ENOTNP, ESIZE = range(7)
+
+GATE1 = {"pauliX": 0, "pauliY": 1, "pauliZ": 2, "hadamard": 3, "phase": 4,
+         "rotateX": 5, "rotateY": 6, "rotateZ": 7}
+GATE2 = {"controlNot": 16, "controlY": 17, "controlZ": 18, "controlRotateX": 19,
+         "controlRotateY": 20, "controlRotateZ": 21, "controlPhase": 22,
+         "controlHadamard": 23, "swap": 24, "fswap": 25, "npRotateX": 26,
+         "npRotateY": 27, "npHadamard": 28}
+ANGLED = {"phase", "rotateX", "rotateY", "rotateZ", "controlRotateX", "controlRotateY",
+          "controlRotateZ", "controlPhase", "npRotateX", "npRotateY"}
+NP_GATES = ("pauliZ", "rotateZ", "phase", "controlZ", "controlRotateZ", "controlPhase",
+            "swap", "fswap", "npRotateX", "npRotateY", "npHadamard")
+
+# every symbol include/qslc.h declares, with its ctypes signature
+_VP = C.c_void_p
+SIGNATURES = {
+    "qslc_version": (C.c_int, []),
+    "qslc_last_error": (C.c_char_p, []),
+    "qslc_create": (C.c_int, [C.c_uint, C.c_int, C.POINTER(C.c_void_p)]),
+    "qslc_create_np": (C.c_int, [C.c_uint, C.c_uint, C.c_int, C.POINTER(C.c_void_p)]),
+    "qslc_destroy": (C.c_int, [_VP]),
+    "qslc_clone": (C.c_int, [_VP, C.POINTER(C.c_void_p)]),
+    "qslc_assign": (C.c_int, [_VP, _VP]),
+    "qslc_num_qubits": (C.c_uint, [_VP]),
+    "qslc_is_np": (C.c_int, [_VP]),
+    "qslc_dtype": (C.c_int, [_VP]),
+    "qslc_num_stored": (C.c_uint64, [_VP]),
+    "qslc_num_ones": (C.c_int, [_VP, C.POINTER(C.c_uint)]),
+    "qslc_set_num_ones": (C.c_int, [_VP, C.c_uint]),
+    "qslc_reset": (C.c_int, [_VP]),
+    "qslc_set_state": (C.c_int, [_VP, _VP, C.c_uint64]),
+    "qslc_get_state": (C.c_int, [_VP, _VP, C.c_uint64]),
+    "qslc_set_basis": (C.c_int, [_VP, C.c_uint64]),
+    "qslc_gate1": (C.c_int, [_VP, C.c_int, C.c_uint, C.c_double]),
+    "qslc_gate2": (C.c_int, [_VP, C.c_int, C.c_uint, C.c_uint, C.c_double]),
+    "qslc_prob": (C.c_int, [_VP, C.c_uint, C.c_uint, C.POINTER(C.c_double)]),
+    "qslc_collapse": (C.c_int, [_VP, C.c_uint, C.c_uint, C.c_double]),
+    "qslc_measure": (C.c_int, [_VP, C.c_uint, C.c_double, C.POINTER(C.c_int)]),
+    "qslc_postselect": (C.c_int, [_VP, C.c_uint, C.c_uint, C.POINTER(C.c_double)]),
+    "qslc_sample": (C.c_int, [_VP, C.c_uint, _VP, C.c_uint64, _VP]),
+    "qslc_sample_all": (C.c_int, [_VP, _VP, C.c_uint64, _VP]),
+    "qslc_measure_all": (C.c_int, [_VP, C.c_double, C.POINTER(C.c_uint64)]),
+    "qslc_set_stream": (C.c_int, [_VP, _VP]),
+    "qslc_get_stream": (C.c_void_p, [_VP]),
+    "qslc_synchronize": (C.c_int, [_VP]),
+    "qslc_launch_count": (C.c_uint64, [_VP]),
+}
+
+
+class QslcError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"qslc error {code}: {msg}")
+        self.code = code
+
+
+class LogicError(QslcError, ValueError):
+    """Raised where the reference throws std::logic_error."""
+
+
+_lib = None
+
+
+def lib(path: str | None = None):
+    """Load libqslc.so (building it first if it is absent and nvcc is present)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        from . import build as _b
+        _b.build()
+    L = C.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc: int) -> None:
+    if rc != OK:
+        msg = lib().qslc_last_error().decode(errors="replace")
+        if rc in (ESIZE, ENOTNP, EINVAL):
+            raise LogicError(rc, msg)
+        raise QslcError(rc, msg)
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+class Qubits:
+    """qsl::Qubits on the GPU: the Default-backend member API over the C ABI.
+
+    ``dtype`` is ``np.complex128`` (qsl::complex<double>) or ``np.complex64``
+    (qsl::complex<float>).  Methods that draw random numbers in the
+    reference (``measure``, ``measureAll``, ``sample``, ``sampleAll``) take
+    the uniforms explicitly, or draw them from ``self.rng``.
+    """
+
+    _np = False
+
+    def __init__(self, nqubits=None, dtype=np.complex128, state=None, seed=None, _handle=None):
+        self.L = lib()
+        self.dtype = np.dtype(dtype)
+        self.code = C128 if self.dtype == np.complex128 else C64
+        self.rng = np.random.default_rng(seed)
+        if _handle is not None:
+            self.h = _handle
+            return
+        if state is not None:
+            state = np.ascontiguousarray(state, dtype=self.dtype)
+            n = state.size.bit_length() - 1
+            if state.size != 1 << n:
+                raise LogicError(ESIZE, "State vector size is not a power of two")
+            nqubits = n
+        h = C.c_void_p()
+        _check(self._create(nqubits, h))
+        self.h = h
+        if state is not None:
+            self.setState(state)
+
+    def _create(self, n, h):
+        return self.L.qslc_create(n, self.code, C.byref(h))
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            self.L.qslc_destroy(h)
+            self.h = None
+
+    def copy(self) -> "Qubits":
+        """Qubits(const Qubits&): a deep copy on the device."""
+        h = C.c_void_p()
+        _check(self.L.qslc_clone(self.h, C.byref(h)))
+        q = object.__new__(type(self))
+        Qubits.__init__(q, dtype=self.dtype, _handle=h)
+        q.rng = np.random.default_rng()
+        return q
+
+    def assign(self, other: "Qubits") -> None:
+        """operator=(const Qubits&)."""
+        _check(self.L.qslc_assign(self.h, other.h))
+
+    # -- state -------------------------------------------------------------
+    def getNumQubits(self) -> int:
+        return int(self.L.qslc_num_qubits(self.h))
+
+    @property
+    def nqubits(self) -> int:
+        return self.getNumQubits()
+
+    def reset(self) -> None:
+        _check(self.L.qslc_reset(self.h))
+
+    def getState(self) -> np.ndarray:
+        out = np.empty(1 << self.nqubits, dtype=self.dtype)
+        _check(self.L.qslc_get_state(self.h, _ptr(out), out.size))
+        return out
+
+    def setState(self, state) -> None:
+        st = np.ascontiguousarray(state, dtype=self.dtype)
+        _check(self.L.qslc_set_state(self.h, _ptr(st), st.size))
+
+    def setBasisState(self, index: int) -> None:
+        _check(self.L.qslc_set_basis(self.h, index))
+
+    def print(self) -> None:
+        print(f"Number of qubits = {self.nqubits}")
+        for a in self.getState():
+            print(f"{a.real} {a.imag}")
+
+    # -- gates -------------------------------------------------------------
+    def gate(self, name: str, q1: int, q2: int | None = None, angle: float = 0.0) -> None:
+        if name in GATE1:
+            _check(self.L.qslc_gate1(self.h, GATE1[name], q1, float(angle)))
+        elif name in GATE2:
+            _check(self.L.qslc_gate2(self.h, GATE2[name], q1, q2, float(angle)))
+        else:
+            raise LogicError(EINVAL, f"unknown gate {name}")
+
+    def synchronize(self) -> None:
+        _check(self.L.qslc_synchronize(self.h))
+
+    def launches(self) -> int:
+        return int(self.L.qslc_launch_count(self.h))
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        _check(self.L.qslc_set_stream(self.h, stream_ptr))
+
+    # -- measurement -------------------------------------------------------
+    def prob(self, targ: int, outcome: int) -> float:
+        out = C.c_double()
+        _check(self.L.qslc_prob(self.h, targ, outcome, C.byref(out)))
+        return out.value
+
+    def postselect(self, targ: int, outcome: int) -> float:
+        out = C.c_double()
+        _check(self.L.qslc_postselect(self.h, targ, outcome, C.byref(out)))
+        return out.value
+
+    def measure(self, targ: int, u: float | None = None) -> int:
+        if u is None:
+            u = self.rng.random()
+        out = C.c_int()
+        _check(self.L.qslc_measure(self.h, targ, float(u), C.byref(out)))
+        return out.value
+
+    def measureAll(self, u: float | None = None) -> int:
+        if u is None:
+            u = self.rng.random()
+        out = C.c_uint64()
+        _check(self.L.qslc_measure_all(self.h, float(u), C.byref(out)))
+        return int(out.value)
+
+    def sample_shots(self, uniforms) -> np.ndarray:
+        """The basis index each uniform draws (the shots behind sampleAll)."""
+        u = np.ascontiguousarray(uniforms, dtype=np.float64)
+        out = np.empty(u.size, dtype=np.uint64)
+        _check(self.L.qslc_sample_all(self.h, _ptr(u), u.size, _ptr(out)))
+        return out
+
+    def sampleAll(self, nsamples: int, uniforms=None) -> dict:
+        u = self.rng.random(nsamples) if uniforms is None else uniforms
+        shots = self.sample_shots(u)
+        keys, counts = np.unique(shots, return_counts=True)
+        return {int(k): int(c) for k, c in zip(keys, counts)}
+
+    def sample(self, targ: int, nsamples: int, uniforms=None) -> list:
+        u = np.ascontiguousarray(self.rng.random(nsamples) if uniforms is None else uniforms,
+                                 dtype=np.float64)
+        counts = np.zeros(2, dtype=np.uint64)
+        _check(self.L.qslc_sample(self.h, targ, _ptr(u), u.size, _ptr(counts)))
+        return [int(counts[0]), int(counts[1])]
+
+
+def _mk(name):
+    if name in GATE1:
+        if name in ANGLED:
+            def f(self, targ, angle):
+                _check(self.L.qslc_gate1(self.h, GATE1[name], targ, float(angle)))
+        else:
+            def f(self, targ):
+                _check(self.L.qslc_gate1(self.h, GATE1[name], targ, 0.0))
+    else:
+        if name in ANGLED:
+            def f(self, q1, q2, angle):
+                _check(self.L.qslc_gate2(self.h, GATE2[name], q1, q2, float(angle)))
+        else:
+            def f(self, q1, q2):
+                _check(self.L.qslc_gate2(self.h, GATE2[name], q1, q2, 0.0))
+    f.__name__ = name
+    return f
+
+
+for _g in list(GATE1) + list(GATE2):
+    setattr(Qubits, _g, _mk(_g))
+
+
+class QubitsNP(Qubits):
+    """qsl::Qubits<Type::NP>: a fixed Hamming weight, stored compressed."""
+
+    _np = True
+
+    def __init__(self, nqubits=None, nones=1, dtype=np.complex128, state=None, seed=None,
+                 _handle=None):
+        self._nones = nones
+        super().__init__(nqubits, dtype=dtype, state=state, seed=seed, _handle=_handle)
+
+    def _create(self, n, h):
+        return self.L.qslc_create_np(n, self._nones, self.code, C.byref(h))
+
+    def getNumOnes(self) -> int:
+        out = C.c_uint()
+        _check(self.L.qslc_num_ones(self.h, C.byref(out)))
+        return out.value
+
+    def setNumOnes(self, nones: int) -> None:
+        _check(self.L.qslc_set_num_ones(self.h, nones))
+
+    def num_stored(self) -> int:
+        return int(self.L.qslc_num_stored(self.h))

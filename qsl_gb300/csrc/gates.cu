@@ -1,0 +1,310 @@
+// gates.cu -- amplitude-pair sweeps of the plain (2^n) layout.
+//
+// One thread owns one amplitude pair (or one amplitude for the diagonal
+// gates) in a grid-stride loop.  The pair index j is turned into the basis
+// index by inserting the target bit (bit insertion replaces the reference's
+// nested s/r loops, gates.cpp:36-37, and its triple i/j/k loops for two
+// qubits, :227-231); consecutive threads touch consecutive 16-byte
+// amplitudes, so every warp reads and writes whole 32-byte sectors for any
+// target above 0.
+//
+// Arithmetic is the reference's, operation for operation, with no
+// contraction into FMA: the x86-64 reference rounds each product and each
+// sum, and so does every update below (rn<T>::mul/add/sub/div).
+#include "qslc_internal.cuh"
+
+#include <cmath>
+
+namespace qslc {
+namespace {
+
+enum PairOp { P_SWAP, P_Y, P_H, P_RX, P_RY, P_RZ };
+enum DiagOp { D_NEG, D_PHASE };
+
+template <class T>
+struct Coef {
+    T c, s;  // cos/sin of angle/2 (rotations) or of angle (phase); sqrt2 for H
+};
+
+template <class T, int OP>
+__device__ __forceinline__ void pair_update(cplx<T> &a0, cplx<T> &a1, const Coef<T> k)
+{
+    using R = rn<T>;
+    cplx<T> r0, r1;
+    if constexpr (OP == P_SWAP) {            // gates.cpp:41, :236, :524
+        r0 = a1;
+        r1 = a0;
+    } else if constexpr (OP == P_Y) {        // gates.cpp:59-62, :267-270
+        r0.x = a1.y; r0.y = -a1.x;
+        r1.x = -a0.y; r1.y = a0.x;
+    } else if constexpr (OP == P_H) {        // gates.cpp:95-98, :493-496, :675-678
+        r0.x = R::div(R::add(a0.x, a1.x), k.c);
+        r0.y = R::div(R::add(a0.y, a1.y), k.c);
+        r1.x = R::div(R::sub(a0.x, a1.x), k.c);
+        r1.y = R::div(R::sub(a0.y, a1.y), k.c);
+    } else if constexpr (OP == P_RX) {       // gates.cpp:139-144, :336-341, :595-600
+        r0.x = R::add(R::mul(a0.x, k.c), R::mul(a1.y, k.s));
+        r0.y = R::sub(R::mul(a0.y, k.c), R::mul(a1.x, k.s));
+        r1.x = R::add(R::mul(a1.x, k.c), R::mul(a0.y, k.s));
+        r1.y = R::sub(R::mul(a1.y, k.c), R::mul(a0.x, k.s));
+    } else if constexpr (OP == P_RY) {       // gates.cpp:169-174, :380-385, :638-643
+        r0.x = R::sub(R::mul(a0.x, k.c), R::mul(a1.x, k.s));
+        r0.y = R::sub(R::mul(a0.y, k.c), R::mul(a1.y, k.s));
+        r1.x = R::add(R::mul(a0.x, k.s), R::mul(a1.x, k.c));
+        r1.y = R::add(R::mul(a0.y, k.s), R::mul(a1.y, k.c));
+    } else {                                 // P_RZ: gates.cpp:200-205, :424-429
+        r0.x = R::add(R::mul(a0.x, k.c), R::mul(a0.y, k.s));
+        r0.y = R::sub(R::mul(a0.y, k.c), R::mul(a0.x, k.s));
+        r1.x = R::sub(R::mul(a1.x, k.c), R::mul(a1.y, k.s));
+        r1.y = R::add(R::mul(a1.y, k.c), R::mul(a1.x, k.s));
+    }
+    a0 = r0;
+    a1 = r1;
+}
+
+template <class T, int OP>
+__device__ __forceinline__ void diag_update(cplx<T> &a, const Coef<T> k)
+{
+    using R = rn<T>;
+    if constexpr (OP == D_NEG) {             // gates.cpp:76-77, :296-297 (x *= -1)
+        a.x = R::mul(a.x, T(-1));
+        a.y = R::mul(a.y, T(-1));
+    } else {                                 // gates.cpp:114-115, :460-461
+        T x = a.x, y = a.y;
+        a.x = R::sub(R::mul(k.c, x), R::mul(k.s, y));
+        a.y = R::add(R::mul(k.c, y), R::mul(k.s, x));
+    }
+}
+
+// One-qubit pair gates: pairs (i0, i0 + 2^t), i0 = insert0(j, t).
+template <class T, int OP>
+__global__ void __launch_bounds__(256) k_pair1(cplx<T> *__restrict__ st, uint64_t npairs,
+                                               unsigned t, Coef<T> k)
+{
+    const uint64_t bit = uint64_t(1) << t;
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < npairs; j += stride) {
+        uint64_t i0 = insert0(j, t);
+        cplx<T> a0 = st[i0], a1 = st[i0 | bit];
+        pair_update<T, OP>(a0, a1, k);
+        st[i0] = a0;
+        st[i0 | bit] = a1;
+    }
+}
+
+// One-qubit diagonal gates on the |1> half: index insert0(j, t) | 2^t.
+template <class T, int OP>
+__global__ void __launch_bounds__(256) k_diag1(cplx<T> *__restrict__ st, uint64_t count,
+                                               unsigned t, Coef<T> k)
+{
+    const uint64_t bit = uint64_t(1) << t;
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < count; j += stride) {
+        uint64_t i = insert0(j, t) | bit;
+        cplx<T> a = st[i];
+        diag_update<T, OP>(a, k);
+        st[i] = a;
+    }
+}
+
+// rotateZ touches both halves with different coefficients; it is a pair
+// gate whose two members do not mix (gates.cpp:181-209).
+
+// Two-qubit gates: j in [0, 2^(n-2)), base = j with zeros inserted at lo < hi.
+// MODE 0: controlled pair (base|b1, base|b1|b2), b1 = control bit;
+// MODE 1: number-preserving pair (base|b1, base|b2);
+// MODE 2: fswap = MODE 1 swap plus negation of base|b1|b2.
+template <class T, int OP, int MODE>
+__global__ void __launch_bounds__(256) k_pair2(cplx<T> *__restrict__ st, uint64_t nquads,
+                                               unsigned lo, unsigned hi, uint64_t b1,
+                                               uint64_t b2, Coef<T> k)
+{
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < nquads; j += stride) {
+        uint64_t base = insert00(j, lo, hi);
+        uint64_t x1 = base | b1;
+        uint64_t x2 = (MODE == 0) ? (x1 | b2) : (base | b2);
+        cplx<T> a0 = st[x1], a1 = st[x2];
+        pair_update<T, OP>(a0, a1, k);
+        st[x1] = a0;
+        st[x2] = a1;
+        if constexpr (MODE == 2) {
+            uint64_t x3 = base | b1 | b2;
+            cplx<T> a = st[x3];
+            diag_update<T, D_NEG>(a, k);
+            st[x3] = a;
+        }
+    }
+}
+
+// controlZ / controlPhase: the |11> quarter (gates.cpp:277-301, :436-465).
+template <class T, int OP>
+__global__ void __launch_bounds__(256) k_diag2(cplx<T> *__restrict__ st, uint64_t nquads,
+                                               unsigned lo, unsigned hi, uint64_t both,
+                                               Coef<T> k)
+{
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < nquads; j += stride) {
+        uint64_t i = insert00(j, lo, hi) | both;
+        cplx<T> a = st[i];
+        diag_update<T, OP>(a, k);
+        st[i] = a;
+    }
+}
+
+// collapse (measure.cpp:31-57): keep half scaled by `factor`, other half zero.
+template <class T>
+__global__ void __launch_bounds__(256) k_collapse(cplx<T> *__restrict__ st, uint64_t npairs,
+                                                  unsigned t, unsigned outcome, T factor)
+{
+    const uint64_t bit = uint64_t(1) << t;
+    const uint64_t keep = outcome ? bit : 0, drop = outcome ? 0 : bit;
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < npairs; j += stride) {
+        uint64_t i = insert0(j, t);
+        cplx<T> a = st[i | keep];
+        a.x = rn<T>::mul(a.x, factor);
+        a.y = rn<T>::mul(a.y, factor);
+        st[i | keep] = a;
+        cplx<T> z;
+        z.x = T(0);
+        z.y = T(0);
+        st[i | drop] = z;
+    }
+}
+
+template <class T>
+__global__ void k_set_one(cplx<T> *st, uint64_t pos)
+{
+    cplx<T> one;
+    one.x = T(1);
+    one.y = T(0);
+    st[pos] = one;
+}
+
+// Host-side coefficients, computed exactly as the reference does: in Fp,
+// with std::cos/std::sin of angle/2 (gates.cpp:124-125) or of angle
+// (:106), and sqrt2 = Fp(std::sqrt(2)) (:94).
+template <class T>
+Coef<T> half_angle(double angle)
+{
+    T a = T(angle);
+    return Coef<T>{T(std::cos(a / 2)), T(std::sin(a / 2))};
+}
+template <class T>
+Coef<T> full_angle(double angle)
+{
+    T a = T(angle);
+    return Coef<T>{T(std::cos(a)), T(std::sin(a))};
+}
+template <class T>
+Coef<T> sqrt2_coef()
+{
+    return Coef<T>{T(std::sqrt(2)), T(0)};
+}
+
+template <class T>
+int gate1_t(qslc_state *s, int gate, unsigned t, double angle)
+{
+    auto *st = static_cast<cplx<T> *>(s->amps);
+    const uint64_t half = uint64_t(1) << (s->n - 1);
+    const unsigned grid = grid_for(half);
+    cudaStream_t str = s->stream;
+    switch (gate) {
+    case QSLC_PAULI_X: k_pair1<T, P_SWAP><<<grid, 256, 0, str>>>(st, half, t, Coef<T>{}); break;
+    case QSLC_PAULI_Y: k_pair1<T, P_Y><<<grid, 256, 0, str>>>(st, half, t, Coef<T>{}); break;
+    case QSLC_HADAMARD: k_pair1<T, P_H><<<grid, 256, 0, str>>>(st, half, t, sqrt2_coef<T>()); break;
+    case QSLC_ROTATE_X: k_pair1<T, P_RX><<<grid, 256, 0, str>>>(st, half, t, half_angle<T>(angle)); break;
+    case QSLC_ROTATE_Y: k_pair1<T, P_RY><<<grid, 256, 0, str>>>(st, half, t, half_angle<T>(angle)); break;
+    case QSLC_ROTATE_Z: k_pair1<T, P_RZ><<<grid, 256, 0, str>>>(st, half, t, half_angle<T>(angle)); break;
+    case QSLC_PAULI_Z: k_diag1<T, D_NEG><<<grid, 256, 0, str>>>(st, half, t, Coef<T>{}); break;
+    case QSLC_PHASE: k_diag1<T, D_PHASE><<<grid, 256, 0, str>>>(st, half, t, full_angle<T>(angle)); break;
+    default: return fail(QSLC_EINVAL, "unknown one-qubit gate code " + std::to_string(gate));
+    }
+    s->launches++;
+    QSLC_CUDA(cudaGetLastError());
+    return QSLC_OK;
+}
+
+template <class T>
+int gate2_t(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle)
+{
+    auto *st = static_cast<cplx<T> *>(s->amps);
+    const uint64_t quads = uint64_t(1) << (s->n - 2);
+    const unsigned lo = q1 < q2 ? q1 : q2, hi = q1 < q2 ? q2 : q1;
+    const uint64_t b1 = uint64_t(1) << q1, b2 = uint64_t(1) << q2;
+    const unsigned grid = grid_for(quads);
+    cudaStream_t str = s->stream;
+#define P2(OP, MODE, K) k_pair2<T, OP, MODE><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1, b2, K)
+    switch (gate) {
+    case QSLC_CONTROL_NOT: P2(P_SWAP, 0, Coef<T>{}); break;
+    case QSLC_CONTROL_Y: P2(P_Y, 0, Coef<T>{}); break;
+    case QSLC_CONTROL_ROTATE_X: P2(P_RX, 0, half_angle<T>(angle)); break;
+    case QSLC_CONTROL_ROTATE_Y: P2(P_RY, 0, half_angle<T>(angle)); break;
+    case QSLC_CONTROL_ROTATE_Z: P2(P_RZ, 0, half_angle<T>(angle)); break;
+    case QSLC_CONTROL_HADAMARD: P2(P_H, 0, sqrt2_coef<T>()); break;
+    case QSLC_SWAP: P2(P_SWAP, 1, Coef<T>{}); break;
+    case QSLC_NP_ROTATE_X: P2(P_RX, 1, half_angle<T>(angle)); break;
+    case QSLC_NP_ROTATE_Y: P2(P_RY, 1, half_angle<T>(angle)); break;
+    case QSLC_NP_HADAMARD: P2(P_H, 1, sqrt2_coef<T>()); break;
+    case QSLC_FSWAP: P2(P_SWAP, 2, Coef<T>{}); break;
+    case QSLC_CONTROL_Z:
+        k_diag2<T, D_NEG><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1 | b2, Coef<T>{});
+        break;
+    case QSLC_CONTROL_PHASE:
+        k_diag2<T, D_PHASE><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1 | b2, full_angle<T>(angle));
+        break;
+    default: return fail(QSLC_EINVAL, "unknown two-qubit gate code " + std::to_string(gate));
+    }
+#undef P2
+    s->launches++;
+    QSLC_CUDA(cudaGetLastError());
+    return QSLC_OK;
+}
+
+}  // namespace
+
+int launch_gate1(qslc_state *s, int gate, unsigned targ, double angle)
+{
+    return s->dtype == QSLC_C128 ? gate1_t<double>(s, gate, targ, angle)
+                                 : gate1_t<float>(s, gate, targ, angle);
+}
+
+int launch_gate2(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle)
+{
+    return s->dtype == QSLC_C128 ? gate2_t<double>(s, gate, q1, q2, angle)
+                                 : gate2_t<float>(s, gate, q1, q2, angle);
+}
+
+int launch_collapse(qslc_state *s, unsigned targ, unsigned outcome, double factor)
+{
+    const uint64_t half = uint64_t(1) << (s->n - 1);
+    const unsigned grid = grid_for(half);
+    if (s->dtype == QSLC_C128)
+        k_collapse<double><<<grid, 256, 0, s->stream>>>(static_cast<double2 *>(s->amps), half, targ,
+                                                        outcome, factor);
+    else
+        k_collapse<float><<<grid, 256, 0, s->stream>>>(static_cast<float2 *>(s->amps), half, targ,
+                                                       outcome, float(factor));
+    s->launches++;
+    QSLC_CUDA(cudaGetLastError());
+    return QSLC_OK;
+}
+
+// All amplitudes zero except `pos`, which becomes 1 (default.cpp:57-65, :80-90).
+int launch_fill_basis(qslc_state *s, uint64_t pos)
+{
+    if (!s->amps || pos >= s->namps)
+        return fail(QSLC_EINVAL, "basis position " + std::to_string(pos) + " outside the " +
+                                     std::to_string(s->namps) + " stored amplitudes");
+    QSLC_CUDA(cudaMemsetAsync(s->amps, 0, s->namps * s->amp_bytes(), s->stream));
+    if (s->dtype == QSLC_C128)
+        k_set_one<double><<<1, 1, 0, s->stream>>>(static_cast<double2 *>(s->amps), pos);
+    else
+        k_set_one<float><<<1, 1, 0, s->stream>>>(static_cast<float2 *>(s->amps), pos);
+    s->launches++;
+    QSLC_CUDA(cudaGetLastError());
+    return QSLC_OK;
+}
+
+}  // namespace qslc

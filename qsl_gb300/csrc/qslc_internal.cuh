@@ -1,0 +1,152 @@
+// qslc_internal.cuh -- shared definitions of the CUDA state-vector backend.
+//
+// Layout in HBM: one contiguous array of complex amplitudes, {re, im}
+// interleaved (qsl::complex<Fp>, include/qsl/utils/complex.hpp:40-49 of
+// qsl), 16 B per amplitude for complex128 and 8 B for complex64.  A plain
+// state holds all 2^n amplitudes; a number-preserving (NP) state holds only
+// the C(n, w) amplitudes of Hamming weight w, in ascending order of their
+// basis index (the order of qsl's generateLookup, src/utils/misc.cpp:75-90).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <string>
+
+#include "qslc.h"
+
+namespace qslc {
+
+// ---------------------------------------------------------------------------
+// Errors: every entry point returns a status; the message is kept per thread.
+// ---------------------------------------------------------------------------
+void set_error(const std::string &msg);
+int fail(int code, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+
+#define QSLC_CUDA(call)                                   \
+    do {                                                  \
+        cudaError_t e_ = (call);                          \
+        if (e_ != cudaSuccess) return qslc::cuda_fail(e_, #call); \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// Round-to-nearest arithmetic with no contraction: qsl's x86-64 build rounds
+// every product and every sum on its own, and so must we to produce the
+// same bits.
+// ---------------------------------------------------------------------------
+template <class T> struct rn;
+template <> struct rn<double> {
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+    static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
+};
+template <> struct rn<float> {
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+};
+
+template <class T> struct cplx_t;
+template <> struct cplx_t<double> { using type = double2; };
+template <> struct cplx_t<float> { using type = float2; };
+template <class T> using cplx = typename cplx_t<T>::type;
+
+// ---------------------------------------------------------------------------
+// Bit insertion: the pair index j in [0, 2^(n-1)) becomes the basis index
+// with a 0 at bit t; the reference's nested (s, r) loops (gates.cpp:36-37)
+// visit the same indices in the same order.
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ uint64_t insert0(uint64_t j, unsigned t)
+{
+    uint64_t low = j & ((uint64_t(1) << t) - 1);
+    return ((j >> t) << (t + 1)) | low;
+}
+// two zero bits at lo < hi
+__host__ __device__ __forceinline__ uint64_t insert00(uint64_t j, unsigned lo, unsigned hi)
+{
+    return insert0(insert0(j, lo), hi);
+}
+
+// ---------------------------------------------------------------------------
+// The state object behind a qslc_state handle.
+// ---------------------------------------------------------------------------
+struct Scratch {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t need);   // grows with cudaMalloc; QSLC_EOOM on failure
+    void release();
+};
+
+// Device tables of a number-preserving state (np.cu): the reference's five
+// lookup tables {n-1,w-1}, {n-2,w-1}, {n-2,w-2}, {n-1,w}, {n,w}.
+struct NPTables {
+    unsigned n = 0, w = 0;
+    uint32_t *tab[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    uint64_t len[5] = {0, 0, 0, 0, 0};
+};
+
+}  // namespace qslc
+
+struct qslc_state {
+    unsigned n = 0;           // qubits
+    int dtype = QSLC_C128;    // QSLC_C128 or QSLC_C64
+    int np = 0;               // 1: number-preserving (compressed) layout
+    unsigned nones = 0;       // Hamming weight of an NP state
+    uint64_t namps = 0;       // amplitudes held on the device
+    void *amps = nullptr;     // device amplitudes
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int device = 0;
+    qslc::Scratch scratch;    // reductions, CDF tiles
+    qslc::Scratch scratch2;
+    void *host_pinned = nullptr;  // small device->host results
+    size_t host_pinned_bytes = 0;
+    uint64_t launches = 0;    // kernels launched through this handle
+    qslc::NPTables *npt = nullptr;
+
+    size_t amp_bytes() const { return dtype == QSLC_C128 ? 16 : 8; }
+};
+
+namespace qslc {
+
+// Launch geometry: grid-stride loops over `work` items with 256 threads per
+// CTA and at most 16 resident CTAs per SM on the 152-SM part.
+unsigned sm_count();
+inline unsigned grid_for(uint64_t work, unsigned threads = 256, unsigned per_sm = 16)
+{
+    uint64_t blocks = (work + threads - 1) / threads;
+    uint64_t cap = uint64_t(sm_count()) * per_sm;
+    if (blocks > cap) blocks = cap;
+    if (blocks == 0) blocks = 1;
+    return unsigned(blocks);
+}
+
+int ensure_pinned(qslc_state *s, size_t bytes);
+
+// gates.cu
+int launch_gate1(qslc_state *s, int gate, unsigned targ, double angle);
+int launch_gate2(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle);
+int launch_collapse(qslc_state *s, unsigned targ, unsigned outcome, double factor);
+int launch_fill_basis(qslc_state *s, uint64_t pos);
+
+// measure.cu
+int seq_prob(qslc_state *s, unsigned targ, unsigned outcome, double *out);
+int seq_sample_all(qslc_state *s, const double *u_host, uint64_t nshots, uint64_t *out_host);
+
+// np.cu
+int np_init_tables();
+int np_prepare(qslc_state *s, unsigned w);   // build the tables for weight w
+void np_release(qslc_state *s);
+int np_gate(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle);
+int np_collapse(qslc_state *s, unsigned targ, unsigned outcome, double factor);
+int np_prob(qslc_state *s, unsigned targ, unsigned outcome, double *out);
+int np_sample_all(qslc_state *s, const double *u, uint64_t n, uint64_t *out);
+int np_expand(qslc_state *s, void *host_full);
+int np_compress(qslc_state *s, const void *host_full, unsigned w);
+uint64_t np_choose(unsigned n, unsigned k);
+uint64_t np_rank_host(uint64_t x);
+
+}  // namespace qslc

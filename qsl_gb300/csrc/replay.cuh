@@ -1,0 +1,158 @@
+// replay.cuh -- exact replay of qsl's sequential floating-point sums.
+//
+// qsl computes prob() and the sampling CDF with a running sum in index
+// order, s <- RN(s + p_i) (src/qubits/default/measure.cpp:60-78, :126-147).
+// A parallel reduction rounds differently, which moves measurement outcomes
+// and, at 2^30 amplitudes, about one shot in a thousand to a neighbouring
+// basis state.  This header holds the pieces that reproduce the sequential
+// sum exactly while the amplitudes are read in parallel:
+//
+//   While the running sum stays inside one binade [2^e, 2^(e+1)) it lives on
+//   the grid of step u_e = ulp(2^e), and each rounded add moves it by
+//   u_e * rne(p / u_e) grid steps, an integer that does not depend on s
+//   (except for exact ties, which depend on the parity of s / u_e).  A tile
+//   of consecutive terms therefore advances the sum by u_e * D with
+//   D = sum of those integers, as long as the sum neither starts outside
+//   binade e nor reaches 2^(e+1) inside the tile and no tie occurs.  Tiles
+//   that break one of these conditions (a handful per sum: the ones where
+//   the running sum crosses a power of two) are replayed term by term.
+//
+// Everything here is __host__ __device__ so the same code runs in the
+// kernels and in the host sequencer.
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+
+#ifdef __CUDACC__
+#define QSLC_HD __host__ __device__ __forceinline__
+#else
+#define QSLC_HD inline
+#endif
+
+namespace qslc {
+
+template <class A> struct fp_traits;
+template <> struct fp_traits<double> {
+    using bits_t = uint64_t;
+    static constexpr int MANT = 52;       // stored mantissa bits
+    static constexpr int BIAS = 1023;
+    static constexpr int EMIN = -1022;    // smallest normal binade
+    static constexpr int EXPMASK = 0x7FF;
+};
+template <> struct fp_traits<float> {
+    using bits_t = uint32_t;
+    static constexpr int MANT = 23;
+    static constexpr int BIAS = 127;
+    static constexpr int EMIN = -126;
+    static constexpr int EXPMASK = 0xFF;
+};
+
+template <class A>
+QSLC_HD typename fp_traits<A>::bits_t to_bits(A x)
+{
+    typename fp_traits<A>::bits_t b;
+#ifdef __CUDA_ARCH__
+    if constexpr (sizeof(A) == 8) b = (uint64_t)__double_as_longlong(x);
+    else b = (uint32_t)__float_as_uint(x);
+#else
+    std::memcpy(&b, &x, sizeof(A));
+#endif
+    return b;
+}
+
+// Binade of a positive normal x: the e with 2^e <= x < 2^(e+1).  Returns
+// EMIN - 1 for zero and subnormals (no binade the fast path can use).
+template <class A>
+QSLC_HD int binade(A x)
+{
+    using T = fp_traits<A>;
+    auto b = to_bits(x);
+    int ef = int((b >> T::MANT) & T::EXPMASK);
+    if (ef == 0) return T::EMIN - 1;
+    return ef - T::BIAS;
+}
+
+// Integer number of grid steps of binade e that adding p >= 0 moves a sum
+// lying in binade e: rne(p / u_e) with u_e = 2^(e - MANT).  `tie` is set
+// when p / u_e is exactly half-way between two integers (the result then
+// depends on the parity of the sum).  `big` is set when the step count does
+// not fit the binade (p itself reaches 2^(e+1)).
+template <class A>
+QSLC_HD uint64_t grid_steps(A p, int e, bool &tie, bool &big)
+{
+    using T = fp_traits<A>;
+    tie = false;
+    big = false;
+    auto b = to_bits(p);
+    int ef = int((b >> T::MANT) & T::EXPMASK);
+    uint64_t m = uint64_t(b & ((typename T::bits_t(1) << T::MANT) - 1));
+    if (ef == 0 && m == 0) return 0;
+    int lsb;                                  // exponent of m's last bit
+    if (ef != 0) {
+        m |= uint64_t(1) << T::MANT;
+        lsb = ef - T::BIAS - T::MANT;
+    } else {
+        lsb = T::EMIN - T::MANT;
+    }
+    int sh = (e - T::MANT) - lsb;             // p / u_e = m * 2^-sh
+    if (sh <= 0) {
+        // exact multiple of the grid; 2^(MANT+1) steps or more leave the binade
+        int ls = -sh;
+        if (ls > T::MANT + 1 || (m >> (T::MANT + 1 - ls)) != 0) { big = true; return 0; }
+        return m << ls;
+    }
+    if (sh >= 64) return 0;                   // m < 2^53 <= half a step
+    uint64_t q = m >> sh;
+    uint64_t rem = m & ((uint64_t(1) << sh) - 1);
+    uint64_t half = uint64_t(1) << (sh - 1);
+    if (rem == half) tie = true;
+    return q + (rem > half ? 1 : 0);
+}
+
+// |a|^2 as the reference computes it: RN(RN(re*re) + RN(im*im))
+// (measure.cpp:69-70, :141-142).
+QSLC_HD double norm2_rn(double re, double im)
+{
+#ifdef __CUDA_ARCH__
+    return __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im));
+#else
+    volatile double a = re * re;   // volatile: no contraction on FMA hosts
+    volatile double b = im * im;
+    return a + b;
+#endif
+}
+QSLC_HD float norm2_rn(float re, float im)
+{
+#ifdef __CUDA_ARCH__
+    return __fadd_rn(__fmul_rn(re, re), __fmul_rn(im, im));
+#else
+    volatile float a = re * re;
+    volatile float b = im * im;
+    return a + b;
+#endif
+}
+
+// Error-free double-double accumulation (Knuth's TwoSum); only an estimate
+// of the exact prefix is needed, to guess each tile's binade.
+struct dd {
+    double hi, lo;
+};
+QSLC_HD dd dd_add(dd a, double b)
+{
+    double s = a.hi + b;
+    double bb = s - a.hi;
+    double err = (a.hi - (s - bb)) + (b - bb);
+    double lo = a.lo + err;
+    double hi = s + lo;
+    return dd{hi, lo - (hi - s)};
+}
+QSLC_HD dd dd_add(dd a, dd b)
+{
+    dd r = dd_add(a, b.hi);
+    r.lo += b.lo;
+    double hi = r.hi + r.lo;
+    return dd{hi, r.lo - (hi - r.hi)};
+}
+
+}  // namespace qslc

@@ -1,0 +1,491 @@
+// seqsum.cuh -- bit-exact sequential sums and CDF sampling over a state.
+//
+// A "producer" describes the sequence the reference sums: element j of
+// the sequence is |a|^2 of one stored amplitude, and index(j) is the basis
+// index it stands for.  prob(targ, outcome) sums the amplitudes whose bit
+// `targ` equals `outcome` in ascending index order (measure.cpp:126-147);
+// the sampling CDF sums every amplitude in ascending order
+// (measure.cpp:60-78).
+//
+// The sum is computed in three device passes over tiles of SEQ_TILE
+// consecutive elements plus a host walk over per-tile metadata:
+//   1. k_seq_tile_sum: an estimate of each tile's sum;
+//   2. the host turns the estimates into a guess of the binade the running
+//      sum occupies in each tile; k_seq_tile_steps counts, per tile, the
+//      grid steps of that binade (replay.cuh) and flags ties;
+//   3. the host walks the tiles in order, advancing the exact running sum by
+//      u_e * D for every tile whose guess holds and replaying the others
+//      term by term (their terms fetched with k_seq_fetch);
+//   4. for sampling, k_seq_resolve rebuilds the exact partial sums inside
+//      each tile that received a shot and finds, for each uniform u, the
+//      first element with partial sum >= u: the reference's binary search
+//      over its Dist vector (measure.cpp:164-188) returns the same element.
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <unordered_map>
+#include <utility>
+#include <vector>
+
+#include "qslc_internal.cuh"
+#include "replay.cuh"
+
+namespace qslc {
+
+constexpr int SEQ_TILE = 4096;
+constexpr int SEQ_TPB = 256;
+constexpr int SEQ_PER = SEQ_TILE / SEQ_TPB;
+constexpr int SEQ_FETCH_CAP = 256;   // tiles fetched per batch for host replay
+
+// ---------------------------------------------------------------------------
+// Producers over the plain 2^n layout.
+// ---------------------------------------------------------------------------
+template <class T>
+struct ProdHalf {        // amplitudes with bit t == outcome, ascending
+    const cplx<T> *amps;
+    unsigned t;
+    uint64_t obit;
+    __device__ __forceinline__ uint64_t index(uint64_t j) const { return insert0(j, t) | obit; }
+    __device__ __forceinline__ T p(uint64_t j) const
+    {
+        cplx<T> a = amps[index(j)];
+        return norm2_rn(a.x, a.y);
+    }
+};
+
+template <class T>
+struct ProdAll {         // every amplitude, ascending
+    const cplx<T> *amps;
+    __device__ __forceinline__ uint64_t index(uint64_t j) const { return j; }
+    __device__ __forceinline__ T p(uint64_t j) const
+    {
+        cplx<T> a = amps[j];
+        return norm2_rn(a.x, a.y);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Kernels.  Element j of tile b is b*SEQ_TILE + k*SEQ_TPB + threadIdx.x for
+// k = 0..SEQ_PER-1, so every load instruction of a warp is coalesced.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum_d(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ uint64_t warp_sum_u(uint64_t v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <class Prod>
+__global__ void __launch_bounds__(SEQ_TPB) k_seq_tile_sum(Prod pr, uint64_t count, uint64_t ntiles,
+                                                          double *__restrict__ out)
+{
+    __shared__ double red[SEQ_TPB / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint64_t b = blockIdx.x; b < ntiles; b += gridDim.x) {
+        double acc = 0;
+        const uint64_t base = b * SEQ_TILE;
+#pragma unroll 4
+        for (int k = 0; k < SEQ_PER; k++) {
+            uint64_t j = base + uint64_t(k) * SEQ_TPB + threadIdx.x;
+            if (j < count) acc += double(pr.p(j));
+        }
+        acc = warp_sum_d(acc);
+        if (lane == 0) red[warp] = acc;
+        __syncthreads();
+        if (warp == 0) {
+            double v = lane < SEQ_TPB / 32 ? red[lane] : 0.0;
+            v = warp_sum_d(v);
+            if (lane == 0) out[b] = v;
+        }
+        __syncthreads();
+    }
+}
+
+template <class Prod, class A>
+__global__ void __launch_bounds__(SEQ_TPB) k_seq_tile_steps(Prod pr, uint64_t count, uint64_t ntiles,
+                                                            const int16_t *__restrict__ guess,
+                                                            uint64_t *__restrict__ steps,
+                                                            uint8_t *__restrict__ flags)
+{
+    __shared__ uint64_t red[SEQ_TPB / 32];
+    __shared__ unsigned fl_all;
+    constexpr uint64_t CAP = uint64_t(1) << (fp_traits<A>::MANT + 1);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint64_t b = blockIdx.x; b < ntiles; b += gridDim.x) {
+        if (threadIdx.x == 0) fl_all = 0;
+        __syncthreads();
+        const int e = guess[b];
+        const uint64_t base = b * SEQ_TILE;
+        uint64_t acc = 0;
+        unsigned fl = 0;
+#pragma unroll 4
+        for (int k = 0; k < SEQ_PER; k++) {
+            uint64_t j = base + uint64_t(k) * SEQ_TPB + threadIdx.x;
+            if (j < count) {
+                bool tie, big;
+                acc += grid_steps<A>(A(pr.p(j)), e, tie, big);
+                fl |= (tie ? 1u : 0u) | (big ? 2u : 0u);
+            }
+        }
+        if (acc >= CAP) {       // saturate: the tile cannot stay in binade e
+            acc = CAP;
+            fl |= 2u;
+        }
+        acc = warp_sum_u(acc);
+        if (fl) atomicOr(&fl_all, fl);
+        if (lane == 0) red[warp] = acc;
+        __syncthreads();
+        if (warp == 0) {
+            uint64_t v = lane < SEQ_TPB / 32 ? red[lane] : 0;
+            v = warp_sum_u(v);
+            if (lane == 0) {
+                steps[b] = v;
+                flags[b] = uint8_t(fl_all);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <class Prod, class P>
+__global__ void __launch_bounds__(SEQ_TPB) k_seq_fetch(Prod pr, uint64_t count,
+                                                       const uint64_t *__restrict__ tiles, int ntl,
+                                                       P *__restrict__ out)
+{
+    for (int q = blockIdx.x; q < ntl; q += gridDim.x) {
+        const uint64_t base = tiles[q] * SEQ_TILE;
+        for (int i = threadIdx.x; i < SEQ_TILE; i += SEQ_TPB) {
+            uint64_t j = base + i;
+            out[uint64_t(q) * SEQ_TILE + i] = j < count ? pr.p(j) : P(0);
+        }
+    }
+}
+
+struct ResolveItem {
+    uint64_t tile;
+    double start;       // exact running sum before the tile's first element
+    int32_t binade;     // binade the sum stays in throughout the tile
+    uint32_t shot0;     // first shot (index into the sorted uniforms)
+    uint32_t nshot;
+    uint32_t pad;
+};
+
+template <class Prod, class A>
+__global__ void __launch_bounds__(SEQ_TPB) k_seq_resolve(Prod pr, uint64_t count,
+                                                         const ResolveItem *__restrict__ items,
+                                                         int nitems,
+                                                         const double *__restrict__ u_sorted,
+                                                         uint64_t *__restrict__ out_sorted)
+{
+    __shared__ uint64_t pre[SEQ_TILE];
+    __shared__ uint64_t wsum[SEQ_TPB / 32];
+    constexpr int MANT = fp_traits<A>::MANT;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int q = blockIdx.x; q < nitems; q += gridDim.x) {
+        const ResolveItem it = items[q];
+        const uint64_t base = it.tile * SEQ_TILE;
+        for (int k = 0; k < SEQ_PER; k++) {
+            int i = k * SEQ_TPB + threadIdx.x;
+            uint64_t j = base + i;
+            uint64_t st = 0;
+            if (j < count) {
+                bool tie, big;
+                st = grid_steps<A>(A(pr.p(j)), it.binade, tie, big);
+            }
+            pre[i] = st;
+        }
+        __syncthreads();
+        // inclusive prefix: each thread owns SEQ_PER consecutive elements
+        uint64_t loc[SEQ_PER];
+        uint64_t run = 0;
+#pragma unroll
+        for (int k = 0; k < SEQ_PER; k++) {
+            run += pre[threadIdx.x * SEQ_PER + k];
+            loc[k] = run;
+        }
+        uint64_t x = run;   // inclusive warp scan of thread totals
+        for (int o = 1; o < 32; o <<= 1) {
+            uint64_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        uint64_t off = x - run;
+        for (int w = 0; w < warp; w++) off += wsum[w];
+#pragma unroll
+        for (int k = 0; k < SEQ_PER; k++) pre[threadIdx.x * SEQ_PER + k] = loc[k] + off;
+        __syncthreads();
+        // running sum before the tile, in grid steps of the tile's binade
+        const uint64_t s0 = uint64_t(ldexp(it.start, MANT - it.binade));
+        for (uint32_t k = threadIdx.x; k < it.nshot; k += SEQ_TPB) {
+            const double u = u_sorted[it.shot0 + k];
+            int lo = 0, hi = SEQ_TILE - 1;   // first i with partial(i) >= u
+            while (lo < hi) {
+                int mid = (lo + hi) >> 1;
+                double v = double(A(ldexp(double(s0 + pre[mid]), it.binade - MANT)));
+                if (v >= u) hi = mid;
+                else lo = mid + 1;
+            }
+            const uint64_t last = count - 1 - base;   // the tile's last valid element
+            out_sorted[it.shot0 + k] = pr.index(base + (uint64_t(lo) < last ? uint64_t(lo) : last));
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host sequencer.
+// ---------------------------------------------------------------------------
+template <class A>
+struct SeqOut {
+    A total = A(0);
+    std::vector<A> starts;                                  // per tile
+    std::vector<int16_t> guess;
+    std::unordered_map<uint64_t, std::vector<A>> partials;  // replayed tiles
+    uint64_t replayed = 0;
+};
+
+// Layout of the handle's scratch for one sequence of `ntiles` tiles.
+struct SeqScratch {
+    double *tile_sum;
+    int16_t *guess;
+    uint64_t *steps;
+    uint8_t *flags;
+    uint64_t *fetch_ids;
+    void *fetch_buf;
+    size_t bytes;
+    static size_t align(size_t x) { return (x + 255) & ~size_t(255); }
+    static SeqScratch carve(void *base, uint64_t ntiles, size_t p_bytes)
+    {
+        SeqScratch s{};
+        char *p = static_cast<char *>(base);
+        size_t off = 0;
+        s.tile_sum = reinterpret_cast<double *>(p + off); off += align(ntiles * 8);
+        s.steps = reinterpret_cast<uint64_t *>(p + off); off += align(ntiles * 8);
+        s.guess = reinterpret_cast<int16_t *>(p + off); off += align(ntiles * 2);
+        s.flags = reinterpret_cast<uint8_t *>(p + off); off += align(ntiles);
+        s.fetch_ids = reinterpret_cast<uint64_t *>(p + off); off += align(SEQ_FETCH_CAP * 8);
+        s.fetch_buf = p + off; off += align(size_t(SEQ_FETCH_CAP) * SEQ_TILE * p_bytes);
+        s.bytes = off;
+        return s;
+    }
+};
+
+template <class A>
+inline A grid_value(uint64_t steps, int e)
+{
+    return A(std::ldexp(double(steps), e - fp_traits<A>::MANT));
+}
+
+// Runs the exact sequential sum of producer `pr` over `count` elements.
+// keep_partials: record every replayed tile's partial sums (for sampling).
+template <class Prod, class P, class A>
+int seq_run(qslc_state *s, const Prod &pr, uint64_t count, bool keep_partials, SeqOut<A> &out)
+{
+    using T = fp_traits<A>;
+    const uint64_t ntiles = (count + SEQ_TILE - 1) / SEQ_TILE;
+    SeqScratch probe = SeqScratch::carve(nullptr, ntiles, sizeof(P));
+    int rc = s->scratch.ensure(probe.bytes);
+    if (rc) return rc;
+    SeqScratch sc = SeqScratch::carve(s->scratch.ptr, ntiles, sizeof(P));
+    cudaStream_t str = s->stream;
+    const unsigned grid = unsigned(std::min<uint64_t>(ntiles, uint64_t(sm_count()) * 8));
+
+    // pass 1: estimates of the tile sums
+    k_seq_tile_sum<Prod><<<grid, SEQ_TPB, 0, str>>>(pr, count, ntiles, sc.tile_sum);
+    s->launches++;
+    QSLC_CUDA(cudaGetLastError());
+    std::vector<double> est(ntiles);
+    QSLC_CUDA(cudaMemcpyAsync(est.data(), sc.tile_sum, ntiles * 8, cudaMemcpyDeviceToHost, str));
+    QSLC_CUDA(cudaStreamSynchronize(str));
+
+    // guesses: the binade of the estimated running sum at each tile start
+    out.guess.assign(ntiles, int16_t(T::EMIN - 1));
+    std::vector<char> predicted(ntiles, 0);
+    {
+        double run = 0;
+        for (uint64_t b = 0; b < ntiles; b++) {
+            const double end = run + est[b];
+            if (est[b] != 0) {
+                int g0 = binade<A>(A(run)), g1 = binade<A>(A(end));
+                out.guess[b] = int16_t(run > 0 ? g0 : g1);
+                // near or across a power of two: expect a replay
+                double nxt = std::ldexp(1.0, (run > 0 ? g0 : g1) + 1);
+                double margin = (sizeof(A) == 8 ? 1e-9 : 1e-4) * nxt;
+                if (run <= 0 || g0 != g1 || end + margin >= nxt || g0 < T::EMIN) predicted[b] = 1;
+            }
+            run = end;
+        }
+    }
+    QSLC_CUDA(cudaMemcpyAsync(sc.guess, out.guess.data(), ntiles * 2, cudaMemcpyHostToDevice, str));
+    k_seq_tile_steps<Prod, A><<<grid, SEQ_TPB, 0, str>>>(pr, count, ntiles, sc.guess, sc.steps, sc.flags);
+    s->launches++;
+    QSLC_CUDA(cudaGetLastError());
+    std::vector<uint64_t> steps(ntiles);
+    std::vector<uint8_t> flags(ntiles);
+    QSLC_CUDA(cudaMemcpyAsync(steps.data(), sc.steps, ntiles * 8, cudaMemcpyDeviceToHost, str));
+    QSLC_CUDA(cudaMemcpyAsync(flags.data(), sc.flags, ntiles, cudaMemcpyDeviceToHost, str));
+    QSLC_CUDA(cudaStreamSynchronize(str));
+
+    // fetch the terms of the tiles expected to need a replay, in batches
+    std::unordered_map<uint64_t, std::vector<P>> terms;
+    auto fetch = [&](const std::vector<uint64_t> &ids) -> int {
+        for (size_t at = 0; at < ids.size(); at += SEQ_FETCH_CAP) {
+            int cnt = int(std::min<size_t>(SEQ_FETCH_CAP, ids.size() - at));
+            QSLC_CUDA(cudaMemcpyAsync(sc.fetch_ids, ids.data() + at, cnt * 8, cudaMemcpyHostToDevice, str));
+            k_seq_fetch<Prod, P><<<unsigned(std::min(cnt, 1024)), SEQ_TPB, 0, str>>>(
+                pr, count, sc.fetch_ids, cnt, static_cast<P *>(sc.fetch_buf));
+            s->launches++;
+            QSLC_CUDA(cudaGetLastError());
+            std::vector<P> buf(size_t(cnt) * SEQ_TILE);
+            QSLC_CUDA(cudaMemcpyAsync(buf.data(), sc.fetch_buf, buf.size() * sizeof(P),
+                                      cudaMemcpyDeviceToHost, str));
+            QSLC_CUDA(cudaStreamSynchronize(str));
+            for (int q = 0; q < cnt; q++)
+                terms[ids[at + q]].assign(buf.begin() + size_t(q) * SEQ_TILE,
+                                          buf.begin() + size_t(q + 1) * SEQ_TILE);
+        }
+        return QSLC_OK;
+    };
+    {
+        std::vector<uint64_t> ids;
+        for (uint64_t b = 0; b < ntiles; b++)
+            if (est[b] != 0 && (predicted[b] || flags[b])) ids.push_back(b);
+        int r = fetch(ids);
+        if (r) return r;
+    }
+
+    // the walk
+    out.starts.assign(ntiles, A(0));
+    out.partials.clear();
+    out.replayed = 0;
+    A sum = A(0);
+    const uint64_t cap = uint64_t(1) << (T::MANT + 1);
+    for (uint64_t b = 0; b < ntiles; b++) {
+        out.starts[b] = sum;
+        if (est[b] == 0) continue;              // every term is zero
+        const int e = out.guess[b];
+        bool ok = flags[b] == 0 && sum > A(0) && binade<A>(sum) == e && e >= T::EMIN;
+        if (ok) {
+            uint64_t s0 = uint64_t(std::ldexp(double(sum), T::MANT - e));
+            ok = s0 + steps[b] < cap;
+            if (ok) {
+                sum = grid_value<A>(s0 + steps[b], e);
+                continue;
+            }
+        }
+        // replay term by term, exactly as the reference adds them
+        auto it = terms.find(b);
+        if (it == terms.end()) {
+            int r = fetch(std::vector<uint64_t>{b});
+            if (r) return r;
+            it = terms.find(b);
+        }
+        const std::vector<P> &t = it->second;
+        std::vector<A> part;
+        if (keep_partials) part.resize(SEQ_TILE);
+        const uint64_t valid = std::min<uint64_t>(SEQ_TILE, count - b * SEQ_TILE);
+        for (uint64_t i = 0; i < valid; i++) {
+            volatile A next = sum + A(t[i]);
+            sum = next;
+            if (keep_partials) part[i] = sum;
+        }
+        for (uint64_t i = valid; keep_partials && i < SEQ_TILE; i++) part[i] = sum;
+        if (keep_partials) out.partials.emplace(b, std::move(part));
+        out.replayed++;
+    }
+    out.total = sum;
+    return QSLC_OK;
+}
+
+// Sampling: for each uniform, the element whose partial sum is the first to
+// reach it.  `host_index` maps an element to its basis index for shots that
+// land in replayed tiles.  Outcomes go to out[0..n) in the order of u.
+template <class Prod, class P, class A, class HostIndex>
+int seq_sample(qslc_state *s, const Prod &pr, uint64_t count, const double *u, uint64_t n,
+               uint64_t *out, HostIndex host_index)
+{
+    SeqOut<A> so;
+    int rc = seq_run<Prod, P, A>(s, pr, count, true, so);
+    if (rc) return rc;
+    const uint64_t ntiles = so.starts.size();
+    std::vector<uint32_t> order(n);
+    for (uint64_t i = 0; i < n; i++) order[i] = uint32_t(i);
+    std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return u[a] < u[b]; });
+    std::vector<double> us(n);
+    for (uint64_t i = 0; i < n; i++) us[i] = u[order[i]];
+
+    std::vector<ResolveItem> items;
+    std::vector<uint64_t> res(n, 0);
+    std::vector<char> on_device(n, 0);
+    uint64_t b = 0;
+    for (uint64_t k = 0; k < n;) {
+        const double uk = us[k];
+        if (uk > double(so.total)) {   // past the total: the reference returns 0 (:167)
+            res[k++] = 0;
+            continue;
+        }
+        // first tile whose end reaches uk
+        while (b < ntiles) {
+            double end = (b + 1 < ntiles) ? double(so.starts[b + 1]) : double(so.total);
+            if (end >= uk) break;
+            b++;
+        }
+        if (b >= ntiles) { res[k++] = 0; continue; }
+        const double end = (b + 1 < ntiles) ? double(so.starts[b + 1]) : double(so.total);
+        uint64_t k1 = k;
+        while (k1 < n && us[k1] <= end) k1++;
+        auto pit = so.partials.find(b);
+        if (pit != so.partials.end()) {
+            const std::vector<A> &part = pit->second;
+            for (uint64_t q = k; q < k1; q++) {
+                uint64_t i = uint64_t(std::lower_bound(part.begin(), part.end(), us[q],
+                                                       [](A v, double x) { return double(v) < x; }) -
+                                      part.begin());
+                if (i >= SEQ_TILE) i = SEQ_TILE - 1;
+                res[q] = host_index(b * SEQ_TILE + i);
+            }
+        } else {
+            ResolveItem it{};
+            it.tile = b;
+            it.start = double(so.starts[b]);
+            it.binade = so.guess[b];
+            it.shot0 = uint32_t(k);
+            it.nshot = uint32_t(k1 - k);
+            items.push_back(it);
+            for (uint64_t q = k; q < k1; q++) on_device[q] = 1;
+        }
+        k = k1;
+    }
+    if (!items.empty()) {
+        const size_t need = SeqScratch::align(n * 8) * 2 + SeqScratch::align(items.size() * sizeof(ResolveItem));
+        rc = s->scratch2.ensure(need);
+        if (rc) return rc;
+        char *p = static_cast<char *>(s->scratch2.ptr);
+        double *d_u = reinterpret_cast<double *>(p);
+        uint64_t *d_out = reinterpret_cast<uint64_t *>(p + SeqScratch::align(n * 8));
+        ResolveItem *d_items = reinterpret_cast<ResolveItem *>(p + 2 * SeqScratch::align(n * 8));
+        cudaStream_t str = s->stream;
+        QSLC_CUDA(cudaMemcpyAsync(d_u, us.data(), n * 8, cudaMemcpyHostToDevice, str));
+        QSLC_CUDA(cudaMemcpyAsync(d_items, items.data(), items.size() * sizeof(ResolveItem),
+                                  cudaMemcpyHostToDevice, str));
+        const unsigned grid = unsigned(std::min<size_t>(items.size(), size_t(sm_count()) * 4));
+        k_seq_resolve<Prod, A><<<grid, SEQ_TPB, 0, str>>>(pr, count, d_items, int(items.size()), d_u, d_out);
+        s->launches++;
+        QSLC_CUDA(cudaGetLastError());
+        std::vector<uint64_t> dev(n);
+        QSLC_CUDA(cudaMemcpyAsync(dev.data(), d_out, n * 8, cudaMemcpyDeviceToHost, str));
+        QSLC_CUDA(cudaStreamSynchronize(str));
+        for (uint64_t q = 0; q < n; q++)
+            if (on_device[q]) res[q] = dev[q];
+    }
+    for (uint64_t q = 0; q < n; q++) out[order[q]] = res[q];
+    return QSLC_OK;
+}
+
+}  // namespace qslc

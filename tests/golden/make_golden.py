@@ -1,0 +1,195 @@
+"""Write the golden fixtures of tests/golden from the reference itself.
+
+Runs qsl's own Default and NP backends (oracle/_ref/libqslref.so: the
+reference sources compiled unmodified, random.cpp replaced by a seedable
+stand-in that can be fed explicit uniforms) on seeded inputs and stores what
+they return.  Needs the reference source tree (it builds oracle/_ref), so it
+runs only where that tree exists; the fixtures it writes are committed and
+travel to the GPU machine.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+from qsl_gb300 import workloads  # noqa: E402
+
+GATES1 = ("pauliX", "pauliY", "pauliZ", "hadamard", "phase", "rotateX", "rotateY", "rotateZ")
+GATES2 = ("controlNot", "controlY", "controlZ", "controlRotateX", "controlRotateY",
+          "controlRotateZ", "controlPhase", "controlHadamard", "swap", "fswap", "npRotateX",
+          "npRotateY", "npHadamard")
+NP_GATES1 = ("pauliZ", "rotateZ", "phase")
+NP_GATES2 = ("controlZ", "controlRotateZ", "controlPhase", "swap", "fswap", "npRotateX",
+             "npRotateY", "npHadamard")
+ALL_NAMES = GATES1 + GATES2
+
+
+def encode(circ):
+    names = np.array([ALL_NAMES.index(g) for g, _, _, _ in circ], dtype=np.int32)
+    q1 = np.array([a for _, a, _, _ in circ], dtype=np.int32)
+    q2 = np.array([-1 if b is None else b for _, _, b, _ in circ], dtype=np.int32)
+    ang = np.array([x for _, _, _, x in circ], dtype=np.float64)
+    return names, q1, q2, ang
+
+
+def decode(names, q1, q2, ang):
+    return [(ALL_NAMES[int(k)], int(a), None if int(b) < 0 else int(b), float(x))
+            for k, a, b, x in zip(names, q1, q2, ang)]
+
+
+def random_circuit(rng, n, gates1, gates2, reps, fp32):
+    circ = []
+    for _ in range(reps):
+        for g in gates1:
+            a = float(rng.uniform(0, 2 * np.pi))
+            if fp32:
+                a = float(np.float32(a))
+            circ.append((g, int(rng.integers(n)), None, a))
+        for g in gates2:
+            q1, q2 = (int(x) for x in rng.choice(n, 2, replace=False))
+            a = float(rng.uniform(0, 2 * np.pi))
+            if fp32:
+                a = float(np.float32(a))
+            circ.append((g, q1, q2, a))
+    rng.shuffle(circ)
+    return circ
+
+
+def feed_map(ref, u):
+    oracle.ref_feed_uniforms(u)
+    m = ref.sample_all(len(u))
+    assert oracle.ref_lib().qslref_uniforms_left() == 0
+    keys = np.array(sorted(m), dtype=np.uint64)
+    return keys, np.array([m[int(k)] for k in keys], dtype=np.uint64)
+
+
+def uniforms(rng, count, fp32):
+    u = rng.random(count)
+    u[u == 0] = 0.5
+    return u.astype(np.float32).astype(np.float64) if fp32 else u
+
+
+def case_default(seed, n, fp32):
+    rng = np.random.default_rng(seed)
+    dt = np.complex64 if fp32 else np.complex128
+    v = rng.uniform(-1, 1, 1 << n) + 1j * rng.uniform(-1, 1, 1 << n)
+    init = (v / np.linalg.norm(v)).astype(dt)
+    circ = random_circuit(rng, n, GATES1, GATES2, 3, fp32)
+    ref = oracle.RefQubits("Default", fp32=fp32, state=init)
+    workloads.apply(ref, circ)
+    final = ref.get_state()
+    probs = np.array([[ref.prob(t, o) for o in (0, 1)] for t in range(n)])
+    u = uniforms(rng, 2000, fp32)
+    keys, counts = feed_map(ref, u)
+    mu = uniforms(rng, 4, fp32)
+    mq = rng.choice(n, 4, replace=False).astype(np.int32)
+    outs = []
+    for q, x in zip(mq, mu):
+        oracle.ref_feed_uniforms([x])
+        outs.append(ref.measure(int(q)))
+    return dict(init=init, final=final, probs=probs, u=u, keys=keys, counts=counts,
+                measure_qubits=mq, measure_u=mu, measure_out=np.array(outs, dtype=np.int32),
+                after_measure=ref.get_state(), **dict(zip(("names", "q1", "q2", "ang"), encode(circ))))
+
+
+def case_np(seed, n, w, fp32):
+    rng = np.random.default_rng(seed)
+    dt = np.complex64 if fp32 else np.complex128
+    init = workloads.np_gaussian_state(n, w, seed, dt)
+    circ = random_circuit(rng, n, NP_GATES1, NP_GATES2, 4, fp32)
+    ref = oracle.RefQubits("NP", fp32=fp32, state=init)
+    workloads.apply(ref, circ)
+    final = ref.get_state()
+    probs = np.array([[ref.prob(t, o) for o in (0, 1)] for t in range(n)])
+    u = uniforms(rng, 2000, fp32)
+    keys, counts = feed_map(ref, u)
+    mu = uniforms(rng, 3, fp32)
+    mq = rng.choice(n, 3, replace=False).astype(np.int32)
+    outs = []
+    for q, x in zip(mq, mu):
+        oracle.ref_feed_uniforms([x])
+        outs.append(ref.measure(int(q)))
+    return dict(init=init, final=final, probs=probs, u=u, keys=keys, counts=counts,
+                measure_qubits=mq, measure_u=mu, measure_out=np.array(outs, dtype=np.int32),
+                after_measure=ref.get_state(), nones=np.int32(w),
+                **dict(zip(("names", "q1", "q2", "ang"), encode(circ))))
+
+
+def case_layered(seed, n, layers, nshots):
+    """The 20-layer hadamard/rotation/phase + controlNot-pairing family,
+    from |0...0>: state, every prob, measureAll on a copy, sampleAll."""
+    rng = np.random.default_rng(seed + 1)
+    circ = workloads.layered_cnot(n, layers, seed)
+    ref = oracle.RefQubits("Default", nqubits=n)
+    workloads.apply(ref, circ)
+    final = ref.get_state()
+    probs = np.array([[ref.prob(t, o) for o in (0, 1)] for t in range(n)])
+    u = uniforms(rng, nshots, False)
+    keys, counts = feed_map(ref, u)
+    ma_u = uniforms(rng, 1, False)
+    copy = oracle.RefQubits("Default", state=final)
+    oracle.ref_feed_uniforms(ma_u)
+    ma = copy.measure_all()
+    return dict(final=final, probs=probs, u=u, keys=keys, counts=counts, measure_all_u=ma_u,
+                measure_all=np.uint64(ma), seed=np.int64(seed), layers=np.int32(layers),
+                **dict(zip(("names", "q1", "q2", "ang"), encode(circ))))
+
+
+def kats():
+    lib = oracle.ref_lib()
+    seq = [0b111]
+    for _ in range(9):
+        seq.append(int(lib.qslref_next(seq[-1])))
+    lookups = {}
+    for length in range(1, 11):
+        for ones in range(0, length + 1):
+            m = lib.qslref_generate_lookup(length, ones, None, 0)
+            out = np.zeros(m, dtype=np.uint64)
+            lib.qslref_generate_lookup(length, ones, out.ctypes.data, m)
+            lookups[f"{length},{ones}"] = [int(x) for x in out]
+    hw = {str(x): int(lib.qslref_hamming_weight(x)) for x in (0b11011010, 0b1010, 0b1, 0)}
+    ch = {f"{a},{b}": int(lib.qslref_choose(a, b)) for a, b in ((1, 1), (4, 3), (10, 3), (10, 10), (28, 14))}
+    return {"next_from_0b111": seq, "lookups": lookups, "hamming_weight": hw, "choose": ch}
+
+
+def main():
+    oracle.build(reference=True)
+    oracle.ref_lib().qslref_seed(12345)
+    for fp32 in (False, True):
+        tag = "c64" if fp32 else "c128"
+        cases = {f"s{s}": case_default(s, 8, fp32) for s in (1, 2, 3)}
+        np.savez_compressed(os.path.join(HERE, f"default_{tag}.npz"),
+                            **{f"{k}__{f}": v for k, c in cases.items() for f, v in c.items()})
+        cases = {"n8w4": case_np(11, 8, 4, fp32), "n10w3": case_np(12, 10, 3, fp32),
+                 "n6w1": case_np(13, 6, 1, fp32)}
+        np.savez_compressed(os.path.join(HERE, f"np_{tag}.npz"),
+                            **{f"{k}__{f}": v for k, c in cases.items() for f, v in c.items()})
+    lay = case_layered(2021, 12, 20, 10000)
+    np.savez_compressed(os.path.join(HERE, "layered_n12.npz"), **lay)
+    with open(os.path.join(HERE, "kat.json"), "w") as f:
+        json.dump(kats(), f, indent=0, sort_keys=True)
+    print("fixtures written to", HERE)
+
+
+def load_cases(path):
+    """{case: {field: array}} from a fixture file written by main()."""
+    z = np.load(path)
+    out = {}
+    for key in z.files:
+        case, field = key.split("__", 1)
+        out.setdefault(case, {})[field] = z[key]
+    return out
+
+
+if __name__ == "__main__":
+    main()
