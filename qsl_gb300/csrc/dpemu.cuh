@@ -1,0 +1,202 @@
+// dpemu.cuh -- IEEE binary64 round-to-nearest-even multiply and add on the
+// integer pipes.
+//
+// GB300 issues two FP64 operations per SM per clock against 64-128 integer
+// operations.  qsl's gate loops round every product and every sum on its
+// own (no FMA), so a dense gate costs 12 FP64 operations per amplitude pair,
+// more than the FP64 pipe can retire at HBM speed.  These routines produce
+// the same bits as __dmul_rn / __dadd_rn from integer arithmetic on the
+// IEEE encodings, so a kernel can split its arithmetic between the FP64 pipe
+// and the integer pipes.
+//
+// Coverage: finite normal operands and results, and zeros.  Anything else
+// (subnormals, infinities, NaNs, a result that would overflow or underflow
+// to a subnormal) reports `ok = false`, and the caller falls back to the
+// native instruction, which is then exact by definition.
+//
+// Methods (textbook binary floating point, e.g. Muller et al., Handbook of
+// Floating-Point Arithmetic, ch. 7-8):
+//   mul: exact 106-bit product of the two 53-bit significands, then
+//        round-to-nearest-even on the guard bit and a sticky bit.
+//   add: align the smaller operand with 10 guard bits, fold every shifted-out
+//        bit into the least significant bit ("jamming"), add or subtract,
+//        renormalise, round to nearest even on the 10 guard bits.  The
+//        jammed bit makes the computed sum odd whenever bits were dropped, so
+//        it can never sit on a rounding tie and always rounds the way the
+//        exact sum does.
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+
+#include "replay.cuh"   // QSLC_HD
+
+namespace qslc {
+namespace emu {
+
+constexpr uint64_t SIGN = 0x8000000000000000ull;
+constexpr uint64_t MANT = 0x000FFFFFFFFFFFFFull;
+constexpr uint64_t HIDDEN = 0x0010000000000000ull;
+
+QSLC_HD uint64_t dbits(double x)
+{
+#ifdef __CUDA_ARCH__
+    return (uint64_t)__double_as_longlong(x);
+#else
+    uint64_t b;
+    std::memcpy(&b, &x, 8);
+    return b;
+#endif
+}
+
+QSLC_HD double dfrom(uint64_t b)
+{
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)b);
+#else
+    double x;
+    std::memcpy(&x, &b, 8);
+    return x;
+#endif
+}
+
+QSLC_HD uint64_t umulhi(uint64_t a, uint64_t b)
+{
+#ifdef __CUDA_ARCH__
+    return __umul64hi(a, b);
+#else
+    return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+QSLC_HD int clz64(uint64_t x)
+{
+#ifdef __CUDA_ARCH__
+    return __clzll((long long)x);
+#else
+    return x ? __builtin_clzll(x) : 64;
+#endif
+}
+
+// A multiplier fixed for a whole kernel (a gate coefficient), decoded once.
+struct MulConst {
+    uint64_t m;      // significand with the hidden bit, 53 bits
+    int e;           // unbiased exponent
+    uint64_t sign;   // SIGN or 0
+    int usable;      // 0: zero/subnormal/inf/nan -- always use the native path
+};
+
+inline MulConst make_const(double c)
+{
+    MulConst k{};
+    uint64_t b;
+    std::memcpy(&b, &c, 8);
+    const int ef = int((b >> 52) & 0x7FF);
+    k.sign = b & SIGN;
+    k.usable = (ef != 0 && ef != 0x7FF) ? 1 : 0;
+    k.m = (b & MANT) | HIDDEN;
+    k.e = ef - 1023;
+    return k;
+}
+
+// RN(a * c) for a normal constant c.  Zeros are exact; the rest needs a
+// normal a and a normal result.
+QSLC_HD uint64_t mul_rn(uint64_t a, const MulConst &c, bool &ok)
+{
+    const uint64_t sign = (a ^ c.sign) & SIGN;
+    const uint64_t aa = a & ~SIGN;
+    if (aa == 0) return sign;                       // +-0 * c
+    const int ef = int(aa >> 52);
+    if (ef == 0 || ef == 0x7FF) {
+        ok = false;
+        return 0;
+    }
+    const uint64_t ma = (aa & MANT) | HIDDEN;
+    // 106-bit product ma * c.m in [2^104, 2^106): hi holds bits 64..105
+    const uint64_t lo = ma * c.m;
+    const uint64_t hi = umulhi(ma, c.m);
+    const int top = int(hi >> 41) & 1;              // leading bit at 105?
+    const int s = 52 + top;                         // bits below the kept 53
+    uint64_t m = (hi << (64 - s)) | (lo >> s);
+    const uint64_t rbit = (lo >> (s - 1)) & 1;
+    const uint64_t sticky = lo & ((uint64_t(1) << (s - 1)) - 1);
+    m += rbit & ((sticky != 0) | (m & 1));
+    int e = ef - 1023 + c.e + top;
+    if (m >> 53) {
+        m >>= 1;
+        e++;
+    }
+    if (e < -1022 || e > 1023) {
+        ok = false;
+        return 0;
+    }
+    return sign | (uint64_t(e + 1023) << 52) | (m & MANT);
+}
+
+// RN(x + y).
+QSLC_HD uint64_t add_rn(uint64_t x, uint64_t y, bool &ok)
+{
+    uint64_t ax = x & ~SIGN, ay = y & ~SIGN;
+    if (ax < ay) {
+        uint64_t t = x; x = y; y = t;
+        t = ax; ax = ay; ay = t;
+    }
+    if (ay == 0) {
+        if (ax != 0) return x;                      // x + 0
+        return x & y & SIGN;                        // +-0 + +-0: -0 only if both are
+    }
+    const int ex = int(ax >> 52), ey = int(ay >> 52);
+    if (ex == 0x7FF || ey == 0) {                   // inf/nan, or a subnormal y (hence x too if ex == 0)
+        ok = false;
+        return 0;
+    }
+    const uint64_t X = ((ax & MANT) | HIDDEN) << 10;   // hidden bit at 62
+    const uint64_t Yf = ((ay & MANT) | HIDDEN) << 10;
+    const int d = ex - ey;
+    uint64_t Y;
+    if (d >= 63) {
+        Y = 1;
+    } else {
+        Y = (Yf >> d) | (uint64_t((Yf & ((uint64_t(1) << d) - 1)) != 0));
+    }
+    uint64_t S;
+    int e = ex;
+    if (((x ^ y) & SIGN) == 0) {
+        S = X + Y;
+        if (S >> 63) {
+            S = (S >> 1) | (S & 1);
+            e++;
+        }
+    } else {
+        S = X - Y;
+        if (S == 0) return 0;                       // x - x = +0
+        const int sh = clz64(S) - 1;
+        S <<= sh;
+        e -= sh;
+    }
+    uint64_t m = S >> 10;
+    const uint64_t rb = S & 0x3FF;
+    m += (rb > 0x200) | ((rb == 0x200) & (m & 1));
+    if (m >> 53) {
+        m >>= 1;
+        e++;
+    }
+    if (e < 1 || e > 2046) {
+        ok = false;
+        return 0;
+    }
+    return (x & SIGN) | (uint64_t(e) << 52) | (m & MANT);
+}
+
+// RN(RN(a*c) + RN(b*s)): the shape of every rotation output in qsl's gate
+// loops (e.g. a0.real*cos + a1.imag*sin, gates.cpp:139).  `ok` reports
+// whether the integer path covered every step.
+QSLC_HD uint64_t dot2_rn(uint64_t a, const MulConst &c, uint64_t b, const MulConst &s, bool &ok)
+{
+    const uint64_t p = mul_rn(a, c, ok);
+    const uint64_t q = mul_rn(b, s, ok);
+    return add_rn(p, q, ok);
+}
+
+}  // namespace emu
+}  // namespace qslc

@@ -17,6 +17,7 @@
 // resulting basis indices to find their slots.  The {n, w} table doubles as
 // the slot -> basis index map used by measurement.
 #include "seqsum.cuh"
+#include "np_host.hpp"
 
 #include <cmath>
 #include <cstring>
@@ -29,23 +30,7 @@ namespace {
 
 constexpr int NP_MAXN = 32;   // the reference's next() is 32-bit (misc.cpp:36)
 __constant__ uint32_t c_binom[NP_MAXN + 1][NP_MAXN + 1];
-// Pascal's triangle up to 33, built on first use (no CUDA involved).
-struct HostBinom {
-    uint64_t v[NP_MAXN + 2][NP_MAXN + 2] = {};
-    HostBinom()
-    {
-        for (int n = 0; n <= NP_MAXN + 1; n++) {
-            v[n][0] = 1;
-            for (int k = 1; k <= n; k++) v[n][k] = v[n - 1][k - 1] + (k <= n - 1 ? v[n - 1][k] : 0);
-        }
-    }
-};
-const HostBinom &hb()
-{
-    static const HostBinom b;
-    return b;
-}
-#define h_binom (hb().v)
+#define h_binom (host_binom().v)
 
 // Partial-rank table, [chunk 0..3][k 0..32][byte value]: 4*33*256 entries.
 constexpr int RT_K = NP_MAXN + 1;
@@ -280,25 +265,9 @@ int init_once()
 // index of table {len, ones} in NPTables::tab
 enum { T_N1W1 = 0, T_N2W1 = 1, T_N2W2 = 2, T_N1W = 3, T_NW = 4 };
 
-uint64_t np_choose(unsigned n, unsigned k)
-{
-    if (k > n || n > NP_MAXN + 1) return 0;
-    return h_binom[n][k];
-}
+uint64_t np_choose(unsigned n, unsigned k) { return choose_u64(n, k); }
 
-uint64_t np_rank_host(uint64_t y)
-{
-    uint64_t r = 0;
-    unsigned t = 0;
-    for (unsigned p = 0; p < 64 && y; p++) {
-        if (y & 1) {
-            t++;
-            r += (t <= p) ? h_binom[p][t] : 0;
-        }
-        y >>= 1;
-    }
-    return r;
-}
+uint64_t np_rank_host(uint64_t y) { return rank_of(y); }
 
 int np_init_tables()
 {
@@ -498,22 +467,8 @@ static int np_sample_t(qslc_state *s, const double *u, uint64_t n, uint64_t *out
     NPTables *tb = tables_of(s);
     ProdNPAll<T> pr{static_cast<const cplx<T> *>(s->amps), tb->tab[T_NW]};
     const unsigned w = s->nones;
-    // slot -> basis index on the host: walk the weight-w integers in order
-    std::vector<uint32_t> cache;
-    auto host_index = [&](uint64_t j) -> uint64_t {
-        // unrank j among the weight-w integers (greedy, combinatorial system)
-        uint64_t x = 0, r = j;
-        unsigned tt = w;
-        for (int p = int(s->n) - 1; p >= 0 && tt > 0; p--) {
-            uint64_t c = np_choose(unsigned(p), tt);
-            if (c <= r) {
-                x |= uint64_t(1) << p;
-                r -= c;
-                tt--;
-            }
-        }
-        return x;
-    };
+    const unsigned nq = s->n;
+    auto host_index = [nq, w](uint64_t j) -> uint64_t { return unrank_of(j, nq, w); };
     return seq_sample<ProdNPAll<T>, T, T>(s, pr, s->namps, u, n, out, host_index);
 }
 
@@ -526,35 +481,18 @@ int np_sample_all(qslc_state *s, const double *u, uint64_t n, uint64_t *out)
 // getState: scatter the slots into a full 2^n host vector, zeros elsewhere.
 int np_expand(qslc_state *s, void *host_full)
 {
-    const size_t ab = s->amp_bytes();
-    std::vector<unsigned char> comp(s->namps * ab);
+    std::vector<unsigned char> comp(s->namps * s->amp_bytes());
     QSLC_CUDA(cudaMemcpyAsync(comp.data(), s->amps, comp.size(), cudaMemcpyDeviceToHost, s->stream));
     QSLC_CUDA(cudaStreamSynchronize(s->stream));
-    unsigned char *full = static_cast<unsigned char *>(host_full);
-    std::memset(full, 0, (size_t(1) << s->n) * ab);
-    uint64_t x = (uint64_t(1) << s->nones) - 1;
-    for (uint64_t r = 0; r < s->namps; r++) {
-        std::memcpy(full + x * ab, comp.data() + r * ab, ab);
-        // Gosper's next (misc.cpp:44-52)
-        uint64_t t = x | (x - 1);
-        x = (t + 1) | (((~t & (~t + 1)) - 1) >> (__builtin_ctzll(x) + 1));
-    }
+    np_scatter(comp.data(), host_full, s->n, s->nones, s->amp_bytes());
     return QSLC_OK;
 }
 
 // setState: gather the weight-w amplitudes (w already validated).
 int np_compress(qslc_state *s, const void *host_full, unsigned w)
 {
-    const size_t ab = s->amp_bytes();
-    const uint64_t cnt = np_choose(s->n, w);
-    std::vector<unsigned char> comp(cnt * ab);
-    const unsigned char *full = static_cast<const unsigned char *>(host_full);
-    uint64_t x = (uint64_t(1) << w) - 1;
-    for (uint64_t r = 0; r < cnt; r++) {
-        std::memcpy(comp.data() + r * ab, full + x * ab, ab);
-        uint64_t t = x | (x - 1);
-        x = (t + 1) | (((~t & (~t + 1)) - 1) >> (__builtin_ctzll(x) + 1));
-    }
+    std::vector<unsigned char> comp(choose_u64(s->n, w) * s->amp_bytes());
+    np_gather(host_full, comp.data(), s->n, w, s->amp_bytes());
     QSLC_CUDA(cudaMemcpyAsync(s->amps, comp.data(), comp.size(), cudaMemcpyHostToDevice, s->stream));
     QSLC_CUDA(cudaStreamSynchronize(s->stream));
     return QSLC_OK;

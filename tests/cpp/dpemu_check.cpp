@@ -1,0 +1,85 @@
+// Checks the integer-pipe binary64 arithmetic (qsl_gb300/csrc/dpemu.cuh)
+// against the host's IEEE multiply and add, bit for bit.  Operands mix
+// random significands with significands that have few set bits (which make
+// exact products, exact sums and rounding ties common), exponent gaps from 0
+// to 70, both signs, zeros, and results near the overflow and underflow
+// thresholds (where the routines must either be exact or decline).
+#include "dpemu.cuh"
+
+#include <cstdio>
+#include <cstdlib>
+#include <random>
+
+using namespace qslc::emu;
+
+static std::mt19937_64 rng(12345);
+
+static double make(int emin, int emax)
+{
+    uint64_t m = rng() & MANT;
+    switch (rng() % 4) {
+    case 0: m &= ~((uint64_t(1) << (rng() % 53)) - 1); break;        // trailing zeros
+    case 1: m = (rng() % 64) << (rng() % 46); m &= MANT; break;         // few bits
+    default: break;
+    }
+    int e = emin + int(rng() % uint64_t(emax - emin + 1));
+    uint64_t b = (uint64_t(e + 1023) << 52) | m | (rng() & 1 ? SIGN : 0);
+    return dfrom(b);
+}
+
+int main(int argc, char **argv)
+{
+    const long N = argc > 1 ? std::atol(argv[1]) : 20000000;
+    long fails = 0, declined_mul = 0, declined_add = 0;
+    for (long i = 0; i < N; i++) {
+        // multiply: constant-like c, amplitude-like a, plus edge exponents
+        double c = (i & 7) == 0 ? make(-1022, 1023) : make(-6, 1);
+        double a = (i & 7) == 1 ? make(-1022, 1023) : make(-80, 2);
+        if ((i & 255) == 3) a = (rng() & 1) ? 0.0 : -0.0;
+        MulConst k = make_const(c);
+        bool ok = true;
+        uint64_t r = mul_rn(dbits(a), k, ok);
+        volatile double ref = a * c;
+        if (ok && r != dbits(ref)) {
+            if (fails++ < 10)
+                std::printf("mul %a * %a: got %a want %a\n", a, c, dfrom(r), (double)ref);
+        }
+        if (!ok) declined_mul++;
+        // add: exponent gap 0..70, both signs
+        double x = make(-60, 3);
+        int gap = int(rng() % 71);
+        uint64_t xb = dbits(x);
+        int ex = int((xb >> 52) & 0x7FF) - 1023;
+        int ey = ex - gap + int(rng() % 3) - 1;
+        if (ey < -1022) ey = -1022;
+        double y = make(ey, ey);
+        if ((i & 255) == 5) y = (rng() & 1) ? 0.0 : -0.0;
+        if ((i & 255) == 6) y = -x;
+        if ((i & 1023) == 7) { x = make(1020, 1023); y = make(1020, 1023); }   // overflow region
+        if ((i & 1023) == 8) { x = make(-1022, -1020); y = -make(-1022, -1020); } // underflow region
+        ok = true;
+        uint64_t s = add_rn(dbits(x), dbits(y), ok);
+        volatile double sref = x + y;
+        if (ok && s != dbits(sref)) {
+            if (fails++ < 10)
+                std::printf("add %a + %a: got %a want %a\n", x, y, dfrom(s), (double)sref);
+        }
+        if (!ok) declined_add++;
+        // the fused shape of a rotation output
+        double b = make(-80, 2), sn = make(-6, 1);
+        MulConst ks = make_const(sn);
+        ok = true;
+        uint64_t d = dot2_rn(dbits(a), k, dbits(b), ks, ok);
+        volatile double p1 = a * c, p2 = b * sn;
+        volatile double dref = p1 + p2;
+        if (ok && d != dbits(dref)) {
+            if (fails++ < 10) std::printf("dot2 mismatch\n");
+        }
+    }
+    std::printf("cases %ld fails %ld declined mul %ld add %ld\n", N, fails, declined_mul, declined_add);
+    if (fails) return 1;
+    // declines must be rare on amplitude-like data
+    if (declined_add > N / 100) return 2;
+    std::puts("dpemu ok");
+    return 0;
+}
