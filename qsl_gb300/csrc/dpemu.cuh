@@ -188,6 +188,69 @@ QSLC_HD uint64_t add_rn(uint64_t x, uint64_t y, bool &ok)
     return (x & SIGN) | (uint64_t(e) << 52) | (m & MANT);
 }
 
+// A divisor fixed for a whole kernel (Hadamard's sqrt(2)), decoded once.
+struct DivConst {
+    uint64_t m;      // significand with the hidden bit
+    uint64_t rinv;   // floor((2^116 - 1) / m): a 64-bit reciprocal
+    int e;           // unbiased exponent
+    uint64_t sign;
+    int usable;
+};
+
+inline DivConst make_div(double y)
+{
+    DivConst k{};
+    uint64_t b;
+    std::memcpy(&b, &y, 8);
+    const int ef = int((b >> 52) & 0x7FF);
+    k.sign = b & SIGN;
+    k.usable = (ef != 0 && ef != 0x7FF) ? 1 : 0;
+    k.m = (b & MANT) | HIDDEN;
+    k.e = ef - 1023;
+    const unsigned __int128 num = ((unsigned __int128)1 << 116) - 1;
+    k.rinv = (uint64_t)(num / k.m);
+    return k;
+}
+
+// RN(x / y) for a normal constant y.  The quotient significand
+// t = floor(mx * 2^k / my) (k = 52 or 53 so that t has 53 bits) is
+// estimated with the reciprocal, which is low by at most one, corrected with
+// the exact remainder r = mx * 2^k - t * my (below 2 * my, so its low 64
+// bits are the whole of it), and rounded to nearest even by comparing 2r
+// with my.
+QSLC_HD uint64_t div_rn(uint64_t x, const DivConst &y, bool &ok)
+{
+    const uint64_t sign = (x ^ y.sign) & SIGN;
+    const uint64_t ax = x & ~SIGN;
+    if (ax == 0) return sign;
+    const int ef = int(ax >> 52);
+    if (ef == 0 || ef == 0x7FF) {
+        ok = false;
+        return 0;
+    }
+    const uint64_t mx = (ax & MANT) | HIDDEN;
+    const int k = mx >= y.m ? 52 : 53;
+    const uint64_t hi = umulhi(mx, y.rinv), lo = mx * y.rinv;
+    uint64_t t = (k == 52) ? hi : ((hi << 1) | (lo >> 63));
+    uint64_t r = (mx << k) - t * y.m;             // exact: the true remainder < 2^54
+    if (r >= y.m) {
+        t++;
+        r -= y.m;
+    }
+    const uint64_t r2 = r << 1;
+    t += (r2 > y.m) | ((r2 == y.m) & (t & 1));
+    int e = ef - 1023 - y.e - k + 52;
+    if (t >> 53) {
+        t >>= 1;
+        e++;
+    }
+    if (e < -1022 || e > 1023) {
+        ok = false;
+        return 0;
+    }
+    return sign | (uint64_t(e + 1023) << 52) | (t & MANT);
+}
+
 // RN(RN(a*c) + RN(b*s)): the shape of every rotation output in qsl's gate
 // loops (e.g. a0.real*cos + a1.imag*sin, gates.cpp:139).  `ok` reports
 // whether the integer path covered every step.

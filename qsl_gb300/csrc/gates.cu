@@ -27,7 +27,28 @@ template <class T>
 struct Coef {
     T c, s;  // cos/sin of angle/2 (rotations) or of angle (phase); sqrt2 for H
     emu::MulConst kc, ks;   // c and s decoded for the integer path (double only)
+    emu::DivConst kd;       // c as a divisor (Hadamard)
 };
+
+// One Hadamard output, RN(RN(a +- b) / sqrt2) (gates.cpp:95-98).  The
+// division always runs on the integer pipes (an FP64 divide is a long
+// iteration on the FP64 pipe); with EMU the sum does too.
+template <class T, bool EMU, bool NEG>
+__device__ __forceinline__ T hdiv(T a, T b, const Coef<T> &k)
+{
+    using R = rn<T>;
+    if constexpr (sizeof(T) == 8) {
+        bool ok = k.kd.usable != 0;
+        if (ok) {
+            uint64_t sb;
+            if constexpr (EMU) sb = emu::add_rn(emu::dbits(a), emu::dbits(b) ^ (NEG ? emu::SIGN : 0), ok);
+            else sb = emu::dbits(NEG ? R::sub(a, b) : R::add(a, b));
+            const uint64_t q = emu::div_rn(sb, k.kd, ok);
+            if (ok) return emu::dfrom(q);
+        }
+    }
+    return R::div(NEG ? R::sub(a, b) : R::add(a, b), k.c);
+}
 
 // One output of a rotation or phase update: RN(RN(a*k1) + RN(b*k2)), or
 // RN(RN(a*k1) - RN(b*k2)) when NEG.  With EMU the integer pipes compute it
@@ -65,10 +86,10 @@ __device__ __forceinline__ void pair_update(cplx<T> &a0, cplx<T> &a1, const Coef
         r0.x = a1.y; r0.y = -a1.x;
         r1.x = -a0.y; r1.y = a0.x;
     } else if constexpr (OP == P_H) {        // gates.cpp:95-98, :493-496, :675-678
-        r0.x = R::div(R::add(a0.x, a1.x), k.c);
-        r0.y = R::div(R::add(a0.y, a1.y), k.c);
-        r1.x = R::div(R::sub(a0.x, a1.x), k.c);
-        r1.y = R::div(R::sub(a0.y, a1.y), k.c);
+        r0.x = hdiv<T, E0, false>(a0.x, a1.x, k);
+        r0.y = hdiv<T, E1, false>(a0.y, a1.y, k);
+        r1.x = hdiv<T, E2, true>(a0.x, a1.x, k);
+        r1.y = hdiv<T, E3, true>(a0.y, a1.y, k);
     } else if constexpr (OP == P_RX) {       // gates.cpp:139-144, :336-341, :595-600
         r0.x = dot2<T, E0, false>(a0.x, k.c, k.kc, a1.y, k.s, k.ks);
         r0.y = dot2<T, E1, true>(a0.y, k.c, k.kc, a1.x, k.s, k.ks);
@@ -220,6 +241,7 @@ Coef<T> coef(T c, T s)
     k.s = s;
     k.kc = emu::make_const(double(c));
     k.ks = emu::make_const(double(s));
+    k.kd = emu::make_div(double(c));
     return k;
 }
 template <class T>
@@ -302,7 +324,9 @@ int gate1_t(qslc_state *s, int gate, unsigned t, double angle)
     switch (gate) {
     case QSLC_PAULI_X: k_pair1<T, P_SWAP><<<grid, 256, 0, str>>>(st, half, t, Coef<T>{}); break;
     case QSLC_PAULI_Y: k_pair1<T, P_Y><<<grid, 256, 0, str>>>(st, half, t, Coef<T>{}); break;
-    case QSLC_HADAMARD: k_pair1<T, P_H><<<grid, 256, 0, str>>>(st, half, t, sqrt2_coef<T>()); break;
+    case QSLC_HADAMARD:
+        WITH_PAIR_MASK(T, (k_pair1<T, P_H, EMV><<<grid, 256, 0, str>>>(st, half, t, sqrt2_coef<T>())));
+        break;
     case QSLC_ROTATE_X:
         WITH_PAIR_MASK(T, (k_pair1<T, P_RX, EMV><<<grid, 256, 0, str>>>(st, half, t, half_angle<T>(angle))));
         break;
@@ -341,11 +365,11 @@ int gate2_t(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle)
     case QSLC_CONTROL_ROTATE_X: P2E(P_RX, 0, half_angle<T>(angle)); break;
     case QSLC_CONTROL_ROTATE_Y: P2E(P_RY, 0, half_angle<T>(angle)); break;
     case QSLC_CONTROL_ROTATE_Z: P2E(P_RZ, 0, half_angle<T>(angle)); break;
-    case QSLC_CONTROL_HADAMARD: P2(P_H, 0, sqrt2_coef<T>()); break;
+    case QSLC_CONTROL_HADAMARD: P2E(P_H, 0, sqrt2_coef<T>()); break;
     case QSLC_SWAP: P2(P_SWAP, 1, Coef<T>{}); break;
     case QSLC_NP_ROTATE_X: P2E(P_RX, 1, half_angle<T>(angle)); break;
     case QSLC_NP_ROTATE_Y: P2E(P_RY, 1, half_angle<T>(angle)); break;
-    case QSLC_NP_HADAMARD: P2(P_H, 1, sqrt2_coef<T>()); break;
+    case QSLC_NP_HADAMARD: P2E(P_H, 1, sqrt2_coef<T>()); break;
     case QSLC_FSWAP: P2(P_SWAP, 2, Coef<T>{}); break;
     case QSLC_CONTROL_Z:
         k_diag2<T, D_NEG><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1 | b2, Coef<T>{});

@@ -250,7 +250,8 @@ struct SeqOut {
     uint64_t replayed = 0;
 };
 
-// Layout of the handle's scratch for one sequence of `ntiles` tiles.
+// Device working storage for one sequence of `ntiles` tiles, carved from
+// one block; `fetch_cap` tiles of terms can be staged for host replay.
 struct SeqScratch {
     double *tile_sum;
     int16_t *guess;
@@ -260,7 +261,7 @@ struct SeqScratch {
     void *fetch_buf;
     size_t bytes;
     static size_t align(size_t x) { return (x + 255) & ~size_t(255); }
-    static SeqScratch carve(void *base, uint64_t ntiles, size_t p_bytes)
+    static SeqScratch carve(void *base, uint64_t ntiles, size_t p_bytes, int fetch_cap)
     {
         SeqScratch s{};
         char *p = static_cast<char *>(base);
@@ -269,11 +270,36 @@ struct SeqScratch {
         s.steps = reinterpret_cast<uint64_t *>(p + off); off += align(ntiles * 8);
         s.guess = reinterpret_cast<int16_t *>(p + off); off += align(ntiles * 2);
         s.flags = reinterpret_cast<uint8_t *>(p + off); off += align(ntiles);
-        s.fetch_ids = reinterpret_cast<uint64_t *>(p + off); off += align(SEQ_FETCH_CAP * 8);
-        s.fetch_buf = p + off; off += align(size_t(SEQ_FETCH_CAP) * SEQ_TILE * p_bytes);
+        s.fetch_ids = reinterpret_cast<uint64_t *>(p + off); off += align(size_t(fetch_cap) * 8);
+        s.fetch_buf = p + off; off += align(size_t(fetch_cap) * SEQ_TILE * p_bytes);
         s.bytes = off;
         return s;
     }
+};
+
+// Host working storage of the walk: per-tile metadata and a small cache of
+// staged tiles (`cap` slots of SEQ_TILE terms each).
+template <class P>
+struct SeqHost {
+    double *est;
+    uint64_t *steps;
+    uint8_t *flags;
+    int16_t *guess;
+    uint8_t *predicted;
+    uint64_t *slot_tile;    // cap entries
+    uint64_t *batch;        // cap entries
+    P *slot_terms;          // cap * SEQ_TILE
+    int cap;
+};
+
+// Where a sequence runs: stream, launch counter, device and host storage.
+template <class P>
+struct SeqEnv {
+    cudaStream_t stream;
+    uint64_t *launches;
+    SeqScratch dev;
+    SeqHost<P> host;
+    int fetch_cap;
 };
 
 template <class A>
@@ -282,125 +308,147 @@ inline A grid_value(uint64_t steps, int e)
     return A(std::ldexp(double(steps), e - fp_traits<A>::MANT));
 }
 
-// Runs the exact sequential sum of producer `pr` over `count` elements.
-// keep_partials: record every replayed tile's partial sums (for sampling).
-template <class Prod, class P, class A>
-int seq_run(qslc_state *s, const Prod &pr, uint64_t count, bool keep_partials, SeqOut<A> &out)
+// The exact sequential sum of producer `pr` over `count` elements.
+// starts (optional, ntiles entries): the running sum before each tile.
+// on_replay (optional): called with (tile, partial sums) for replayed tiles.
+template <class Prod, class P, class A, class OnReplay>
+int seq_core(SeqEnv<P> &env, const Prod &pr, uint64_t count, A *total, A *starts,
+             OnReplay on_replay, uint64_t *replayed)
 {
     using T = fp_traits<A>;
     const uint64_t ntiles = (count + SEQ_TILE - 1) / SEQ_TILE;
-    SeqScratch probe = SeqScratch::carve(nullptr, ntiles, sizeof(P));
-    int rc = s->scratch.ensure(probe.bytes);
-    if (rc) return rc;
-    SeqScratch sc = SeqScratch::carve(s->scratch.ptr, ntiles, sizeof(P));
-    cudaStream_t str = s->stream;
+    SeqScratch &sc = env.dev;
+    SeqHost<P> &h = env.host;
+    cudaStream_t str = env.stream;
     const unsigned grid = unsigned(std::min<uint64_t>(ntiles, uint64_t(sm_count()) * 8));
 
     // pass 1: estimates of the tile sums
     k_seq_tile_sum<Prod><<<grid, SEQ_TPB, 0, str>>>(pr, count, ntiles, sc.tile_sum);
-    s->launches++;
+    (*env.launches)++;
     QSLC_CUDA(cudaGetLastError());
-    std::vector<double> est(ntiles);
-    QSLC_CUDA(cudaMemcpyAsync(est.data(), sc.tile_sum, ntiles * 8, cudaMemcpyDeviceToHost, str));
+    QSLC_CUDA(cudaMemcpyAsync(h.est, sc.tile_sum, ntiles * 8, cudaMemcpyDeviceToHost, str));
     QSLC_CUDA(cudaStreamSynchronize(str));
 
     // guesses: the binade of the estimated running sum at each tile start
-    out.guess.assign(ntiles, int16_t(T::EMIN - 1));
-    std::vector<char> predicted(ntiles, 0);
     {
         double run = 0;
         for (uint64_t b = 0; b < ntiles; b++) {
-            const double end = run + est[b];
-            if (est[b] != 0) {
+            const double end = run + h.est[b];
+            h.guess[b] = int16_t(T::EMIN - 1);
+            h.predicted[b] = 0;
+            if (h.est[b] != 0) {
                 int g0 = binade<A>(A(run)), g1 = binade<A>(A(end));
-                out.guess[b] = int16_t(run > 0 ? g0 : g1);
+                h.guess[b] = int16_t(run > 0 ? g0 : g1);
                 // near or across a power of two: expect a replay
                 double nxt = std::ldexp(1.0, (run > 0 ? g0 : g1) + 1);
                 double margin = (sizeof(A) == 8 ? 1e-9 : 1e-4) * nxt;
-                if (run <= 0 || g0 != g1 || end + margin >= nxt || g0 < T::EMIN) predicted[b] = 1;
+                if (run <= 0 || g0 != g1 || end + margin >= nxt || g0 < T::EMIN) h.predicted[b] = 1;
             }
             run = end;
         }
     }
-    QSLC_CUDA(cudaMemcpyAsync(sc.guess, out.guess.data(), ntiles * 2, cudaMemcpyHostToDevice, str));
+    QSLC_CUDA(cudaMemcpyAsync(sc.guess, h.guess, ntiles * 2, cudaMemcpyHostToDevice, str));
     k_seq_tile_steps<Prod, A><<<grid, SEQ_TPB, 0, str>>>(pr, count, ntiles, sc.guess, sc.steps, sc.flags);
-    s->launches++;
+    (*env.launches)++;
     QSLC_CUDA(cudaGetLastError());
-    std::vector<uint64_t> steps(ntiles);
-    std::vector<uint8_t> flags(ntiles);
-    QSLC_CUDA(cudaMemcpyAsync(steps.data(), sc.steps, ntiles * 8, cudaMemcpyDeviceToHost, str));
-    QSLC_CUDA(cudaMemcpyAsync(flags.data(), sc.flags, ntiles, cudaMemcpyDeviceToHost, str));
+    QSLC_CUDA(cudaMemcpyAsync(h.steps, sc.steps, ntiles * 8, cudaMemcpyDeviceToHost, str));
+    QSLC_CUDA(cudaMemcpyAsync(h.flags, sc.flags, ntiles, cudaMemcpyDeviceToHost, str));
     QSLC_CUDA(cudaStreamSynchronize(str));
 
-    // fetch the terms of the tiles expected to need a replay, in batches
-    std::unordered_map<uint64_t, std::vector<P>> terms;
-    auto fetch = [&](const std::vector<uint64_t> &ids) -> int {
-        for (size_t at = 0; at < ids.size(); at += SEQ_FETCH_CAP) {
-            int cnt = int(std::min<size_t>(SEQ_FETCH_CAP, ids.size() - at));
-            QSLC_CUDA(cudaMemcpyAsync(sc.fetch_ids, ids.data() + at, cnt * 8, cudaMemcpyHostToDevice, str));
-            k_seq_fetch<Prod, P><<<unsigned(std::min(cnt, 1024)), SEQ_TPB, 0, str>>>(
-                pr, count, sc.fetch_ids, cnt, static_cast<P *>(sc.fetch_buf));
-            s->launches++;
-            QSLC_CUDA(cudaGetLastError());
-            std::vector<P> buf(size_t(cnt) * SEQ_TILE);
-            QSLC_CUDA(cudaMemcpyAsync(buf.data(), sc.fetch_buf, buf.size() * sizeof(P),
-                                      cudaMemcpyDeviceToHost, str));
-            QSLC_CUDA(cudaStreamSynchronize(str));
-            for (int q = 0; q < cnt; q++)
-                terms[ids[at + q]].assign(buf.begin() + size_t(q) * SEQ_TILE,
-                                          buf.begin() + size_t(q + 1) * SEQ_TILE);
-        }
+    // Staged terms for replays: a tile that needs one is fetched together
+    // with the next tiles expected to need one, up to `cap` per batch.
+    for (int i = 0; i < h.cap; i++) h.slot_tile[i] = ~uint64_t(0);
+    auto terms_of = [&](uint64_t b, const P **out) -> int {
+        for (int i = 0; i < h.cap; i++)
+            if (h.slot_tile[i] == b) {
+                *out = h.slot_terms + size_t(i) * SEQ_TILE;
+                return QSLC_OK;
+            }
+        int cnt = 0;
+        h.batch[cnt++] = b;
+        for (uint64_t c = b + 1; c < ntiles && cnt < h.cap; c++)
+            if (h.est[c] != 0 && (h.predicted[c] || h.flags[c])) h.batch[cnt++] = c;
+        QSLC_CUDA(cudaMemcpyAsync(sc.fetch_ids, h.batch, size_t(cnt) * 8, cudaMemcpyHostToDevice, str));
+        k_seq_fetch<Prod, P><<<unsigned(std::min(cnt, 1024)), SEQ_TPB, 0, str>>>(
+            pr, count, sc.fetch_ids, cnt, static_cast<P *>(sc.fetch_buf));
+        (*env.launches)++;
+        QSLC_CUDA(cudaGetLastError());
+        QSLC_CUDA(cudaMemcpyAsync(h.slot_terms, sc.fetch_buf, size_t(cnt) * SEQ_TILE * sizeof(P),
+                                  cudaMemcpyDeviceToHost, str));
+        QSLC_CUDA(cudaStreamSynchronize(str));
+        for (int i = 0; i < h.cap; i++) h.slot_tile[i] = i < cnt ? h.batch[i] : ~uint64_t(0);
+        *out = h.slot_terms;
         return QSLC_OK;
     };
-    {
-        std::vector<uint64_t> ids;
-        for (uint64_t b = 0; b < ntiles; b++)
-            if (est[b] != 0 && (predicted[b] || flags[b])) ids.push_back(b);
-        int r = fetch(ids);
-        if (r) return r;
-    }
 
     // the walk
-    out.starts.assign(ntiles, A(0));
-    out.partials.clear();
-    out.replayed = 0;
     A sum = A(0);
+    uint64_t nrep = 0;
     const uint64_t cap = uint64_t(1) << (T::MANT + 1);
     for (uint64_t b = 0; b < ntiles; b++) {
-        out.starts[b] = sum;
-        if (est[b] == 0) continue;              // every term is zero
-        const int e = out.guess[b];
-        bool ok = flags[b] == 0 && sum > A(0) && binade<A>(sum) == e && e >= T::EMIN;
+        if (starts) starts[b] = sum;
+        if (h.est[b] == 0) continue;            // every term is zero
+        const int e = h.guess[b];
+        bool ok = h.flags[b] == 0 && sum > A(0) && binade<A>(sum) == e && e >= T::EMIN;
         if (ok) {
             uint64_t s0 = uint64_t(std::ldexp(double(sum), T::MANT - e));
-            ok = s0 + steps[b] < cap;
+            ok = s0 + h.steps[b] < cap;
             if (ok) {
-                sum = grid_value<A>(s0 + steps[b], e);
+                sum = grid_value<A>(s0 + h.steps[b], e);
                 continue;
             }
         }
         // replay term by term, exactly as the reference adds them
-        auto it = terms.find(b);
-        if (it == terms.end()) {
-            int r = fetch(std::vector<uint64_t>{b});
-            if (r) return r;
-            it = terms.find(b);
-        }
-        const std::vector<P> &t = it->second;
-        std::vector<A> part;
-        if (keep_partials) part.resize(SEQ_TILE);
+        const P *t = nullptr;
+        int r = terms_of(b, &t);
+        if (r) return r;
         const uint64_t valid = std::min<uint64_t>(SEQ_TILE, count - b * SEQ_TILE);
+        const A before = sum;
         for (uint64_t i = 0; i < valid; i++) {
             volatile A next = sum + A(t[i]);
             sum = next;
-            if (keep_partials) part[i] = sum;
         }
-        for (uint64_t i = valid; keep_partials && i < SEQ_TILE; i++) part[i] = sum;
-        if (keep_partials) out.partials.emplace(b, std::move(part));
-        out.replayed++;
+        on_replay(b, before, t, valid);
+        nrep++;
     }
-    out.total = sum;
+    *total = sum;
+    if (replayed) *replayed = nrep;
     return QSLC_OK;
+}
+
+// The same over a handle's growable scratch; the host storage is heap.
+template <class Prod, class P, class A>
+int seq_run(qslc_state *s, const Prod &pr, uint64_t count, bool keep_partials, SeqOut<A> &out)
+{
+    const uint64_t ntiles = (count + SEQ_TILE - 1) / SEQ_TILE;
+    const int cap = SEQ_FETCH_CAP;
+    SeqScratch probe = SeqScratch::carve(nullptr, ntiles, sizeof(P), cap);
+    int rc = s->scratch.ensure(probe.bytes);
+    if (rc) return rc;
+    std::vector<double> est(ntiles);
+    std::vector<uint64_t> steps(ntiles), slot_tile(cap), batch(cap);
+    std::vector<uint8_t> flags(ntiles), predicted(ntiles);
+    out.guess.assign(ntiles, 0);
+    std::vector<P> slot_terms(size_t(cap) * SEQ_TILE);
+    SeqEnv<P> env{s->stream, &s->launches, SeqScratch::carve(s->scratch.ptr, ntiles, sizeof(P), cap),
+                  SeqHost<P>{est.data(), steps.data(), flags.data(), out.guess.data(), predicted.data(),
+                             slot_tile.data(), batch.data(), slot_terms.data(), cap},
+                  cap};
+    out.starts.assign(ntiles, A(0));
+    out.partials.clear();
+    auto on_replay = [&](uint64_t b, A before, const P *t, uint64_t valid) {
+        if (!keep_partials) return;
+        std::vector<A> part(SEQ_TILE);
+        A run = before;
+        for (uint64_t i = 0; i < valid; i++) {
+            volatile A next = run + A(t[i]);
+            run = next;
+            part[i] = run;
+        }
+        for (uint64_t i = valid; i < SEQ_TILE; i++) part[i] = run;
+        out.partials.emplace(b, std::move(part));
+    };
+    return seq_core<Prod, P, A>(env, pr, count, &out.total, out.starts.data(), on_replay, &out.replayed);
 }
 
 // Sampling: for each uniform, the element whose partial sum is the first to

@@ -65,6 +65,28 @@ int main(int argc, char **argv)
                 std::printf("add %a + %a: got %a want %a\n", x, y, dfrom(s), (double)sref);
         }
         if (!ok) declined_add++;
+        // division by a constant: sqrt(2) (Hadamard) and random divisors
+        {
+            double yv = (i & 3) ? 1.4142135623730951 : make(-8, 8);
+            DivConst kd = make_div(yv);
+            double xv = (i & 15) == 9 ? make(-1022, 1023) : make(-80, 3);
+            if ((i & 255) == 10) xv = (rng() & 1) ? 0.0 : -0.0;
+            ok = true;
+            uint64_t qd = div_rn(dbits(xv), kd, ok);
+            volatile double qref = xv / yv;
+            if (ok && qd != dbits(qref)) {
+                if (fails++ < 10) std::printf("div %a / %a: got %a want %a\n", xv, yv, dfrom(qd), (double)qref);
+            }
+            // exact quotients and exact halfway cases: x = q * y for short q
+            double qv = make(-4, 4);
+            double prod = qv * yv;
+            ok = true;
+            qd = div_rn(dbits(prod), kd, ok);
+            volatile double qref2 = prod / yv;
+            if (ok && qd != dbits(qref2)) {
+                if (fails++ < 10) std::printf("div2 %a / %a: got %a want %a\n", prod, yv, dfrom(qd), (double)qref2);
+            }
+        }
         // the fused shape of a rotation output
         double b = make(-80, 2), sn = make(-6, 1);
         MulConst ks = make_const(sn);
