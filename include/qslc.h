@@ -186,6 +186,26 @@ QSLC_API int qslc_synchronize(qslc_state *s);
 /* Kernels launched through this handle since it was created. */
 QSLC_API uint64_t qslc_launch_count(const qslc_state *s);
 
+/* No counterpart in the reference: prob(targ, outcome) for callers that
+ * cannot allocate device memory -- code running inside a framework whose
+ * pool or arena owns every device allocation, code that must not trigger
+ * the device-wide synchronisation cudaMalloc/cudaFree can cause, plugins in
+ * a process that has reserved the whole device.  `amps` is the caller's
+ * device array of 2^nqubits amplitudes (dtype QSLC_C128 or QSLC_C64),
+ * `stream` a cudaStream_t (NULL: the default stream); the result is the
+ * same bits as qslc_prob.  It allocates nothing: its scratch is one
+ * file-scope device array of QSLC_NOALLOC_SCRATCH_BYTES, which every GPU
+ * that loads the library holds until the process exits, shared by all
+ * calls (calls that overlap on the GPU race on it; calls made through this
+ * library in one process are serialised).  States above
+ * QSLC_NOALLOC_MAX_QUBITS qubits are rejected with QSLC_EINVAL.  The first
+ * call on a device looks up the array's address on that device; make it
+ * before any stream capture. */
+#define QSLC_NOALLOC_SCRATCH_BYTES (1u << 20)
+#define QSLC_NOALLOC_MAX_QUBITS 27
+QSLC_API int qslc_prob_noalloc(const void *amps, unsigned nqubits, int dtype, unsigned targ,
+                               unsigned outcome, void *stream, double *out);
+
 #ifdef __cplusplus
 }
 #endif

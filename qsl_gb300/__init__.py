@@ -67,6 +67,8 @@ SIGNATURES = {
     "qslc_get_stream": (C.c_void_p, [_VP]),
     "qslc_synchronize": (C.c_int, [_VP]),
     "qslc_launch_count": (C.c_uint64, [_VP]),
+    "qslc_prob_noalloc": (C.c_int, [_VP, C.c_uint, C.c_int, C.c_uint, C.c_uint, _VP,
+                                    C.POINTER(C.c_double)]),
 }
 
 
