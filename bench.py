@@ -153,6 +153,115 @@ def cpu_sample(circ, n, seconds=20.0, threads=None):
     return done / dt, done, threads
 
 
+def run_fused(args, torch, q, stream):
+    """The precision form (fused FP32 blocks, FP64 norms and CDF): the layered
+    circuit at depth 60 on a 32-qubit complex64 state, k = 5, against the
+    plain FP64 path at the same size; infidelity on a 28-qubit instance."""
+    n, depth, k = args.fused_qubits, 60, 5
+    circ = workloads.layered_mixed(n, depth, SEED + 4)
+    per = n + n // 2
+    warm, timed = circ[:3 * per], circ[3 * per:]
+    sim = q.Qubits(n, dtype=np.complex64)
+    sim.set_stream(stream.cuda_stream)
+    sim.set_fusion(k)
+    workloads.apply(sim, warm)
+    sim.flush()
+    torch.cuda.synchronize()
+    b0 = sim.fused_blocks()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    workloads.apply(sim, timed)
+    sim.flush()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    fused_ms = e0.elapsed_time(e1)
+    blocks = sim.fused_blocks() - b0
+    su = workloads.uniforms(args.shots, SEED + 5)
+    t0 = time.perf_counter()
+    sim.sample_shots(su)
+    sample_ms = (time.perf_counter() - t0) * 1e3
+    del sim
+    torch.cuda.empty_cache()
+    # plain FP64 (complex128) at the same size: one layer
+    plain = q.Qubits(n)
+    plain.set_stream(stream.cuda_stream)
+    workloads.apply(plain, circ[:per])
+    torch.cuda.synchronize()
+    e0.record(stream)
+    workloads.apply(plain, circ[per:2 * per])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_gps = per / (e0.elapsed_time(e1) * 1e-3)
+    del plain
+    # infidelity on a 28-qubit instance against the FP64 path (bit for bit
+    # the reference's Default backend, by the parity tests)
+    m = args.fused_check_qubits
+    c28 = workloads.layered_mixed(m, depth, SEED + 4)
+    ref = q.Qubits(m)
+    workloads.apply(ref, c28)
+    f = q.Qubits(m, dtype=np.complex64)
+    f.set_fusion(k)
+    workloads.apply(f, c28)
+    a = ref.getState()
+    b = f.getState().astype(np.complex128)
+    fid = abs(np.vdot(a, b)) ** 2 / (np.vdot(a, a).real * np.vdot(b, b).real)
+    maxerr = float(np.abs(a - b).max())
+    del ref, f, a, b
+    fused_gps = len(timed) / (fused_ms * 1e-3)
+    return {"nqubits": n, "dtype": "c64 state, FP32 blocks, FP64 norms/CDF", "k": k,
+            "depth": depth, "gates_timed": len(timed), "fused_blocks": blocks,
+            "gates_per_block": len(timed) / max(blocks, 1), "ms": fused_ms,
+            "equivalent_gates_per_s": fused_gps,
+            "plain_fp64_gates_per_s_same_size": plain_gps,
+            "speedup_vs_plain_fp64": fused_gps / plain_gps,
+            "infidelity": 1 - fid, "infidelity_qubits": m, "max_abs_err": maxerr,
+            "sample_shots": args.shots, "sample_ms": sample_ms}
+
+
+def run_np(args, torch, q, stream):
+    """Number-preserving backend: 28 qubits, weight 14, 2000 gates from
+    {npRotateX, swap, phase, controlPhase}; the OpenMP NP restatement of the
+    reference on the host cores beside it."""
+    n, w, ngates = 28, 14, 2000
+    st = workloads.np_gaussian_state(n, w, SEED + 6)
+    circ = workloads.np_mix(n, ngates, SEED + 7)
+    sim = q.QubitsNP(state=st)
+    sim.set_stream(stream.cuda_stream)
+    workloads.apply(sim, circ[:50])
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    workloads.apply(sim, circ)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    touched = 0
+    for g, _, _, _ in circ:
+        from math import comb
+        touched += {"npRotateX": 2 * comb(n - 2, w - 1), "swap": 2 * comb(n - 2, w - 1),
+                    "phase": comb(n - 1, w - 1), "controlPhase": comb(n - 2, w - 2)}[g]
+    out = {"nqubits": n, "nones": w, "gates": ngates, "ms": ms, "gates_per_s": ngates / (ms * 1e-3),
+           "alg_gbs": 32 * touched / (ms * 1e-3) / 1e9, "stored_amplitudes": sim.num_stored()}
+    del sim
+    if not args.no_cpu:
+        import oracle
+        oracle.build(reference=False)
+        thr = os.cpu_count() or 1
+        cpu = oracle.PortNPQubits(n, w, nthreads=thr, state=st)
+        t0 = time.perf_counter()
+        done = 0
+        for g in circ:
+            cpu.gate(*g)
+            done += 1
+            if time.perf_counter() - t0 > args.cpu_seconds / 2:
+                break
+        out["cpu_baseline"] = {"value": done / (time.perf_counter() - t0), "unit": UNIT, "cores": thr,
+                               "kind": "port", "sample": f"first {done} gates, OpenMP NP restatement"}
+    return out
+
+
 def run_gpu(args):
     import torch
     import qsl_gb300 as q
@@ -290,6 +399,12 @@ def run_gpu(args):
     }
     if e2e:
         line["e2e"] = e2e
+    del sim
+    torch.cuda.empty_cache()
+    if not args.no_fused:
+        line["fused"] = run_fused(args, torch, q, stream)
+    if not args.no_np:
+        line["np"] = run_np(args, torch, q, stream)
     if rank == 0 and not args.no_cpu:
         v, done, thr = cpu_sample(circ, n, seconds=args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": thr, "kind": "port",
@@ -357,6 +472,10 @@ def main():
     ap.add_argument("--ref-gates", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fused", action="store_true")
+    ap.add_argument("--no-np", action="store_true")
+    ap.add_argument("--fused-qubits", type=int, default=32)
+    ap.add_argument("--fused-check-qubits", type=int, default=28)
     ap.add_argument("--traffic", type=float, default=None,
                     help="dram bytes per launch of the top kernel from an ncu capture")
     args = ap.parse_args()

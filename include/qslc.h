@@ -186,6 +186,36 @@ QSLC_API int qslc_synchronize(qslc_state *s);
 /* Kernels launched through this handle since it was created. */
 QSLC_API uint64_t qslc_launch_count(const qslc_state *s);
 
+/* Precision form (no counterpart in the reference).  With max_qubits in
+ * 1..5 on a complex64 plain state, gates are queued and, at the next call
+ * that reads or measures the state (or qslc_flush), fused into dense
+ * blocks of at most max_qubits qubits applied as one FP32 sweep each;
+ * prob, measurement decisions, collapse factors and the sampling CDF run in
+ * FP64.  Results then match the FP64 path to FP32 accuracy instead of bit
+ * for bit.  0 turns fusion off (after applying what is queued). */
+QSLC_API int qslc_set_fusion(qslc_state *s, unsigned max_qubits);
+QSLC_API int qslc_flush(qslc_state *s);
+/* Fused blocks applied through this handle so far. */
+QSLC_API uint64_t qslc_fused_blocks(const qslc_state *s);
+
+/* Batching form (no counterpart in the reference).  A batch of `ninst`
+ * independent circuits, instance i on nqubits[i] qubits (2..26) with
+ * nlayers[i] layers of: rotateY on every qubit, rotateZ on every qubit,
+ * controlNot(q, q+1) for q = 0..n-2; then prob(q, 0) and prob(q, 1) for
+ * every q and `nshots` sampleAll draws.  All instances run in one
+ * persistent kernel captured once in a CUDA graph.  Results are the bits
+ * qsl's Default backend gives for the same calls. */
+typedef struct qslc_batch qslc_batch;
+QSLC_API int qslc_batch_create(int dtype, uint32_t ninst, const uint32_t *nqubits,
+                               const uint32_t *nlayers, uint32_t nshots, qslc_batch **out);
+/* angles: per instance, layer-major, per qubit (rotateY angle, rotateZ
+ * angle); uniforms: nshots per instance.  probs: per instance 2*n values
+ * (prob(q,0), prob(q,1)), q ascending; shots: nshots per instance, in the
+ * order of the uniforms. */
+QSLC_API int qslc_batch_run(qslc_batch *b, const double *angles, const double *uniforms,
+                            double *probs, uint64_t *shots);
+QSLC_API int qslc_batch_destroy(qslc_batch *b);
+
 /* No counterpart in the reference: prob(targ, outcome) for callers that
  * cannot allocate device memory -- code running inside a framework whose
  * pool or arena owns every device allocation, code that must not trigger

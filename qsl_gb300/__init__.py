@@ -69,6 +69,13 @@ SIGNATURES = {
     "qslc_launch_count": (C.c_uint64, [_VP]),
     "qslc_prob_noalloc": (C.c_int, [_VP, C.c_uint, C.c_int, C.c_uint, C.c_uint, _VP,
                                     C.POINTER(C.c_double)]),
+    "qslc_set_fusion": (C.c_int, [_VP, C.c_uint]),
+    "qslc_flush": (C.c_int, [_VP]),
+    "qslc_fused_blocks": (C.c_uint64, [_VP]),
+    "qslc_batch_create": (C.c_int, [C.c_int, C.c_uint32, _VP, _VP, C.c_uint32,
+                                    C.POINTER(C.c_void_p)]),
+    "qslc_batch_run": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
+    "qslc_batch_destroy": (C.c_int, [_VP]),
 }
 
 
@@ -214,6 +221,17 @@ class Qubits:
     def set_stream(self, stream_ptr: int | None) -> None:
         _check(self.L.qslc_set_stream(self.h, stream_ptr))
 
+    def set_fusion(self, max_qubits: int) -> None:
+        """Precision form: queue gates and apply them as fused FP32 blocks of
+        at most ``max_qubits`` qubits (complex64 states; 0 turns it off)."""
+        _check(self.L.qslc_set_fusion(self.h, max_qubits))
+
+    def flush(self) -> None:
+        _check(self.L.qslc_flush(self.h))
+
+    def fused_blocks(self) -> int:
+        return int(self.L.qslc_fused_blocks(self.h))
+
     # -- measurement -------------------------------------------------------
     def prob(self, targ: int, outcome: int) -> float:
         out = C.c_double()
@@ -306,3 +324,41 @@ class QubitsNP(Qubits):
 
     def num_stored(self) -> int:
         return int(self.L.qslc_num_stored(self.h))
+
+
+class Batch:
+    """Batching form: many ansatz circuits (rotateY and rotateZ on every qubit,
+    then a controlNot ladder, per layer) in one persistent launch replayed
+    from a CUDA graph; per instance prob(q, 0/1) for every q and shots."""
+
+    def __init__(self, nqubits, nlayers, nshots: int, dtype=np.complex128):
+        self.L = lib()
+        self.n = np.ascontiguousarray(nqubits, dtype=np.uint32)
+        self.layers = np.ascontiguousarray(nlayers, dtype=np.uint32)
+        self.nshots = int(nshots)
+        self.code = C128 if np.dtype(dtype) == np.complex128 else C64
+        h = C.c_void_p()
+        _check(self.L.qslc_batch_create(self.code, self.n.size, _ptr(self.n), _ptr(self.layers),
+                                        self.nshots, C.byref(h)))
+        self.h = h
+        self.angle_count = int(np.sum(2 * self.n.astype(np.int64) * self.layers))
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            self.L.qslc_batch_destroy(h)
+            self.h = None
+
+    def run(self, angles, uniforms):
+        """Returns (probs as a list of (n, 2) arrays, shots as (ninst, nshots))."""
+        a = np.ascontiguousarray(angles, dtype=np.float64)
+        u = np.ascontiguousarray(uniforms, dtype=np.float64)
+        assert a.size == self.angle_count and u.size == self.n.size * self.nshots
+        probs = np.empty(int(2 * self.n.astype(np.int64).sum()), dtype=np.float64)
+        shots = np.empty(self.n.size * self.nshots, dtype=np.uint64)
+        _check(self.L.qslc_batch_run(self.h, _ptr(a), _ptr(u), _ptr(probs), _ptr(shots)))
+        out, at = [], 0
+        for n in self.n:
+            out.append(probs[at:at + 2 * n].reshape(n, 2))
+            at += 2 * n
+        return out, shots.reshape(self.n.size, self.nshots)

@@ -83,6 +83,13 @@ int check_handle(const qslc_state *s)
     return QSLC_OK;
 }
 
+// Apply queued gates of the precision form before the state is read.
+int flushed(qslc_state *s)
+{
+    if (!s->fuse_queue.empty()) return fusion_flush(s);
+    return QSLC_OK;
+}
+
 // (Re)allocate the amplitude array for `count` amplitudes.
 int alloc_amps(qslc_state *s, uint64_t count)
 {
@@ -133,6 +140,7 @@ void free_state(qslc_state *s)
     if (s->amps) cudaFree(s->amps);
     s->scratch.release();
     s->scratch2.release();
+    s->fuse_mats.release();
     if (s->host_pinned) cudaFreeHost(s->host_pinned);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
     delete s;
@@ -254,6 +262,7 @@ int qslc_destroy(qslc_state *s)
 int qslc_clone(const qslc_state *src, qslc_state **out)
 {
     int rc = check_handle(src);
+    if (!rc) rc = flushed(const_cast<qslc_state *>(src));
     if (rc) return rc;
     rc = new_state(src->n, src->dtype, out);
     if (rc) return rc;
@@ -261,6 +270,7 @@ int qslc_clone(const qslc_state *src, qslc_state **out)
     s->np = src->np;
     if (src->np) rc = np_set_weight(s, src->nones);
     else rc = alloc_amps(s, src->namps);
+    if (!rc) s->fuse_k = src->fuse_k;
     if (!rc) {
         cudaStreamSynchronize(src->stream);
         cudaError_t e = cudaMemcpyAsync(s->amps, src->amps, src->namps * src->amp_bytes(),
@@ -283,7 +293,10 @@ int qslc_assign(qslc_state *dst, const qslc_state *src)
         return fail(QSLC_ESIZE, "Cannot assign Qubits object vector from different number of qubits");
     if (dst->dtype != src->dtype || dst->np != src->np)
         return fail(QSLC_EINVAL, "cannot assign between different simulator types");
-    if (dst == src) return QSLC_OK;
+    if (dst == src) return flushed(dst);
+    rc = flushed(const_cast<qslc_state *>(src));
+    if (rc) return rc;
+    dst->fuse_queue.clear();                 // overwritten below
     if (dst->np && dst->nones != src->nones) {
         rc = np_set_weight(dst, src->nones);
         if (rc) return rc;
@@ -322,6 +335,7 @@ int qslc_reset(qslc_state *s)
 {
     int rc = check_handle(s);
     if (rc) return rc;
+    s->fuse_queue.clear();
     return launch_fill_basis(s, 0);
 }
 
@@ -333,6 +347,7 @@ int qslc_set_state(qslc_state *s, const void *amps, uint64_t n_amps)
     if (n_amps != dim)
         return fail(QSLC_ESIZE, "Cannot assign state vector from different number of qubits");
     if (!amps) return fail(QSLC_EINVAL, "null amplitude pointer");
+    s->fuse_queue.clear();
     if (!s->np) {
         QSLC_CUDA(cudaMemcpyAsync(s->amps, amps, dim * s->amp_bytes(), cudaMemcpyHostToDevice, s->stream));
         QSLC_CUDA(cudaStreamSynchronize(s->stream));
@@ -356,6 +371,8 @@ int qslc_get_state(const qslc_state *cs, void *amps, uint64_t n_amps)
     const uint64_t dim = uint64_t(1) << s->n;
     if (n_amps != dim) return fail(QSLC_ESIZE, "output size must be 2^nqubits amplitudes");
     if (!amps) return fail(QSLC_EINVAL, "null amplitude pointer");
+    rc = flushed(s);
+    if (rc) return rc;
     if (s->np) return np_expand(s, amps);
     QSLC_CUDA(cudaMemcpyAsync(amps, s->amps, dim * s->amp_bytes(), cudaMemcpyDeviceToHost, s->stream));
     QSLC_CUDA(cudaStreamSynchronize(s->stream));
@@ -368,6 +385,7 @@ int qslc_set_basis(qslc_state *s, uint64_t index)
     if (rc) return rc;
     if (s->n < 64 && index >= (uint64_t(1) << s->n))
         return fail(QSLC_EINVAL, "basis index out of range");
+    s->fuse_queue.clear();
     if (!s->np) return launch_fill_basis(s, index);
     const unsigned w = unsigned(__builtin_popcountll(index));
     if (w != s->nones) {
@@ -390,6 +408,10 @@ int qslc_gate1(qslc_state *s, int gate, unsigned targ, double angle)
                                          " does not preserve the number of ones");
         return np_gate(s, gate, targ, targ, angle);
     }
+    if (s->fuse_k) {
+        s->fuse_queue.push_back(GateOp{gate, targ, targ, angle});
+        return QSLC_OK;
+    }
     return launch_gate1(s, gate, targ, angle);
 }
 
@@ -408,6 +430,10 @@ int qslc_gate2(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle)
                                          " does not preserve the number of ones");
         return np_gate(s, gate, q1, q2, angle);
     }
+    if (s->fuse_k) {
+        s->fuse_queue.push_back(GateOp{gate, q1, q2, angle});
+        return QSLC_OK;
+    }
     return launch_gate2(s, gate, q1, q2, angle);
 }
 
@@ -417,6 +443,8 @@ int qslc_prob(qslc_state *s, unsigned targ, unsigned outcome, double *out)
     if (!rc) rc = check_q(s, targ);
     if (rc) return rc;
     if (outcome > 1 || !out) return fail(QSLC_EINVAL, "outcome must be 0 or 1");
+    rc = flushed(s);
+    if (rc) return rc;
     return s->np ? np_prob(s, targ, outcome, out) : seq_prob(s, targ, outcome, out);
 }
 
@@ -426,7 +454,11 @@ int qslc_collapse(qslc_state *s, unsigned targ, unsigned outcome, double factor)
     if (!rc) rc = check_q(s, targ);
     if (rc) return rc;
     if (outcome > 1) return fail(QSLC_EINVAL, "outcome must be 0 or 1");
-    return s->np ? np_collapse(s, targ, outcome, factor) : launch_collapse(s, targ, outcome, factor);
+    rc = flushed(s);
+    if (rc) return rc;
+    if (s->np) return np_collapse(s, targ, outcome, factor);
+    if (s->fuse_k && s->dtype == QSLC_C64) return launch_collapse_f64(s, targ, outcome, factor);
+    return launch_collapse(s, targ, outcome, factor);
 }
 
 int qslc_measure(qslc_state *s, unsigned targ, double u, int *outcome)
@@ -436,7 +468,7 @@ int qslc_measure(qslc_state *s, unsigned targ, double u, int *outcome)
     if (rc) return rc;
     int o;
     double factor;
-    if (s->dtype == QSLC_C128) decide<double>(p0, u, &o, &factor);
+    if (s->dtype == QSLC_C128 || s->fuse_k) decide<double>(p0, u, &o, &factor);   // FP64 in the precision form
     else decide<float>(p0, u, &o, &factor);
     rc = qslc_collapse(s, targ, unsigned(o), factor);
     if (rc) return rc;
@@ -450,7 +482,7 @@ int qslc_postselect(qslc_state *s, unsigned targ, unsigned outcome, double *prob
     int rc = qslc_prob(s, targ, outcome, &p);
     if (rc) return rc;
     double factor;
-    if (s->dtype == QSLC_C128) factor = 1 / std::sqrt(p);          // measure.cpp:154-155
+    if (s->dtype == QSLC_C128 || s->fuse_k) factor = 1 / std::sqrt(p);   // measure.cpp:154-155
     else factor = double(1.0f / std::sqrt(float(p)));
     rc = qslc_collapse(s, targ, outcome, factor);
     if (rc) return rc;
@@ -466,7 +498,7 @@ int qslc_sample(qslc_state *s, unsigned targ, const double *u, uint64_t nshots, 
     if (rc) return rc;
     counts[0] = counts[1] = 0;
     for (uint64_t i = 0; i < nshots; i++) {   // measure.cpp:205-213, compared in Fp
-        bool zero = s->dtype == QSLC_C128 ? (u[i] < p0) : (float(u[i]) < float(p0));
+        bool zero = (s->dtype == QSLC_C128 || s->fuse_k) ? (u[i] < p0) : (float(u[i]) < float(p0));
         counts[zero ? 0 : 1]++;
     }
     return QSLC_OK;
@@ -479,7 +511,9 @@ int qslc_sample_all(qslc_state *s, const double *u, uint64_t nshots, uint64_t *o
     if (nshots == 0) return QSLC_OK;
     if (!u || !out) return fail(QSLC_EINVAL, "null pointer");
     if (nshots > 0xFFFFFFFFull) return fail(QSLC_EINVAL, "at most 2^32-1 shots per call");
-    if (s->dtype == QSLC_C64) {
+    rc = flushed(s);
+    if (rc) return rc;
+    if (s->dtype == QSLC_C64 && !s->fuse_k) {
         // the reference draws Fp uniforms; widen the float values exactly
         std::vector<double> uf(nshots);
         for (uint64_t i = 0; i < nshots; i++) uf[i] = double(float(u[i]));
@@ -502,6 +536,7 @@ int qslc_measure_all(qslc_state *s, double u, uint64_t *outcome)
 int qslc_set_stream(qslc_state *s, void *stream)
 {
     int rc = check_handle(s);
+    if (!rc) rc = flushed(s);
     if (rc) return rc;
     QSLC_CUDA(cudaStreamSynchronize(s->stream));
     if (stream == nullptr) {
@@ -522,11 +557,34 @@ void *qslc_get_stream(const qslc_state *s) { return s ? static_cast<void *>(s->s
 int qslc_synchronize(qslc_state *s)
 {
     int rc = check_handle(s);
+    if (!rc) rc = flushed(s);
     if (rc) return rc;
     QSLC_CUDA(cudaStreamSynchronize(s->stream));
     return QSLC_OK;
 }
 
 uint64_t qslc_launch_count(const qslc_state *s) { return s ? s->launches : 0; }
+
+int qslc_set_fusion(qslc_state *s, unsigned max_qubits)
+{
+    int rc = check_handle(s);
+    if (rc) return rc;
+    if (max_qubits > 5) return fail(QSLC_EINVAL, "fusion blocks span at most 5 qubits");
+    if (max_qubits && (s->dtype != QSLC_C64 || s->np))
+        return fail(QSLC_EINVAL, "the fused precision form runs on complex64 plain states");
+    rc = flushed(s);
+    if (rc) return rc;
+    s->fuse_k = max_qubits;
+    return QSLC_OK;
+}
+
+int qslc_flush(qslc_state *s)
+{
+    int rc = check_handle(s);
+    if (rc) return rc;
+    return flushed(s);
+}
+
+uint64_t qslc_fused_blocks(const qslc_state *s) { return s ? s->fused_blocks : 0; }
 
 }  // extern "C"

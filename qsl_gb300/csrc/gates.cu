@@ -221,6 +221,23 @@ __global__ void __launch_bounds__(256) k_collapse(cplx<T> *__restrict__ st, uint
     }
 }
 
+// complex64 amplitudes scaled in double and rounded once (precision form)
+__global__ void __launch_bounds__(256) k_collapse_f64(float2 *__restrict__ st, uint64_t npairs,
+                                                      unsigned t, unsigned outcome, double factor)
+{
+    const uint64_t bit = uint64_t(1) << t;
+    const uint64_t keep = outcome ? bit : 0, drop = outcome ? 0 : bit;
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < npairs; j += stride) {
+        uint64_t i = insert0(j, t);
+        float2 a = st[i | keep];
+        a.x = float(double(a.x) * factor);
+        a.y = float(double(a.y) * factor);
+        st[i | keep] = a;
+        st[i | drop] = make_float2(0.f, 0.f);
+    }
+}
+
 template <class T>
 __global__ void k_set_one(cplx<T> *st, uint64_t pos)
 {
@@ -269,7 +286,7 @@ int emu_mask_pair()
 {
     static int m = [] {
         const char *e = std::getenv("QSLC_EMU_MASK");
-        return e ? std::atoi(e) & 15 : 3;
+        return e ? std::atoi(e) & 15 : 5;
     }();
     return m;
 }
@@ -411,6 +428,16 @@ int launch_collapse(qslc_state *s, unsigned targ, unsigned outcome, double facto
     else
         k_collapse<float><<<grid, 256, 0, s->stream>>>(static_cast<float2 *>(s->amps), half, targ,
                                                        outcome, float(factor));
+    s->launches++;
+    QSLC_CUDA(cudaGetLastError());
+    return QSLC_OK;
+}
+
+int launch_collapse_f64(qslc_state *s, unsigned targ, unsigned outcome, double factor)
+{
+    const uint64_t half = uint64_t(1) << (s->n - 1);
+    k_collapse_f64<<<grid_for(half), 256, 0, s->stream>>>(static_cast<float2 *>(s->amps), half, targ,
+                                                        outcome, factor);
     s->launches++;
     QSLC_CUDA(cudaGetLastError());
     return QSLC_OK;

@@ -11,12 +11,14 @@
 
 namespace qslc {
 
-template <class T>
+// T: amplitude type; A: the running sum (Fp in the reference; double in
+// the precision form, which keeps norms in FP64)
+template <class T, class A>
 static int prob_t(qslc_state *s, unsigned targ, unsigned outcome, double *out)
 {
     ProdHalf<T> pr{static_cast<const cplx<T> *>(s->amps), targ, uint64_t(outcome) << targ};
-    SeqOut<T> so;
-    int rc = seq_run<ProdHalf<T>, T, T>(s, pr, uint64_t(1) << (s->n - 1), false, so);
+    SeqOut<A> so;
+    int rc = seq_run<ProdHalf<T>, T, A>(s, pr, uint64_t(1) << (s->n - 1), false, so);
     if (rc) return rc;
     *out = double(so.total);
     return QSLC_OK;
@@ -24,8 +26,9 @@ static int prob_t(qslc_state *s, unsigned targ, unsigned outcome, double *out)
 
 int seq_prob(qslc_state *s, unsigned targ, unsigned outcome, double *out)
 {
-    return s->dtype == QSLC_C128 ? prob_t<double>(s, targ, outcome, out)
-                                 : prob_t<float>(s, targ, outcome, out);
+    if (s->dtype == QSLC_C128) return prob_t<double, double>(s, targ, outcome, out);
+    if (s->fuse_k) return prob_t<float, double>(s, targ, outcome, out);
+    return prob_t<float, float>(s, targ, outcome, out);
 }
 
 template <class T>

@@ -40,7 +40,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[QSLC_NOALLOC_SC
 
 // Host working storage of the walk, sized for the largest accepted state.
 double h_est[NOALLOC_MAX_TILES];
-uint64_t h_steps[NOALLOC_MAX_TILES];
+uint64_t h_steps[2 * NOALLOC_MAX_TILES];
 uint8_t h_flags[NOALLOC_MAX_TILES];
 int16_t h_guess[NOALLOC_MAX_TILES];
 uint8_t h_pred[NOALLOC_MAX_TILES];

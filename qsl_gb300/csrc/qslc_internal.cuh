@@ -14,6 +14,9 @@
 #include <string>
 
 #include "qslc.h"
+#include "fusion_host.hpp"
+
+#include <vector>
 
 namespace qslc {
 
@@ -106,6 +109,11 @@ struct qslc_state {
     size_t host_pinned_bytes = 0;
     uint64_t launches = 0;    // kernels launched through this handle
     qslc::NPTables *npt = nullptr;
+    // precision form (fused.cu): queued gates, fusion width, block matrices
+    unsigned fuse_k = 0;
+    std::vector<qslc::GateOp> fuse_queue;
+    qslc::Scratch fuse_mats;
+    uint64_t fused_blocks = 0;
 
     size_t amp_bytes() const { return dtype == QSLC_C128 ? 16 : 8; }
 };
@@ -130,7 +138,12 @@ int ensure_pinned(qslc_state *s, size_t bytes);
 int launch_gate1(qslc_state *s, int gate, unsigned targ, double angle);
 int launch_gate2(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle);
 int launch_collapse(qslc_state *s, unsigned targ, unsigned outcome, double factor);
+// complex64 collapse with the factor applied in double (precision form)
+int launch_collapse_f64(qslc_state *s, unsigned targ, unsigned outcome, double factor);
 int launch_fill_basis(qslc_state *s, uint64_t pos);
+
+// fused.cu
+int fusion_flush(qslc_state *s);
 
 // measure.cu
 int seq_prob(qslc_state *s, unsigned targ, unsigned outcome, double *out);

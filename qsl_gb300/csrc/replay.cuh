@@ -110,6 +110,38 @@ QSLC_HD uint64_t grid_steps(A p, int e, bool &tie, bool &big)
     return q + (rem > half ? 1 : 0);
 }
 
+// The effect of a run of terms on a sum in binade e, as grid steps, for
+// either parity of the sum (in grid steps) before the run.  A term whose
+// quotient p / u_e sits exactly half-way (a tie) rounds to the even
+// neighbour, so its step count is q or q + 1 depending on the parity of the
+// sum it lands on; every other term has a fixed count.  Runs compose
+// associatively: (A then B)(par) = A(par) + B(par + A(par)).
+struct Tx {
+    uint64_t d[2];
+};
+QSLC_HD Tx tx_identity() { return Tx{{0, 0}}; }
+QSLC_HD Tx tx_term(uint64_t q, bool tie)
+{
+    if (!tie) return Tx{{q, q}};
+    return Tx{{q + (q & 1), q + ((q + 1) & 1)}};
+}
+// Counts saturate at 2^62: a tile whose count reaches the binade's size
+// is discarded anyway, and saturation keeps such a count from wrapping
+// around to a small value.
+constexpr uint64_t TX_SAT = uint64_t(1) << 62;
+QSLC_HD uint64_t sat_add(uint64_t a, uint64_t b)
+{
+    const uint64_t r = a + b;   // a, b <= 2^62: no wrap
+    return r > TX_SAT ? TX_SAT : r;
+}
+QSLC_HD Tx tx_then(const Tx &a, const Tx &b)
+{
+    Tx r;
+    r.d[0] = sat_add(a.d[0], b.d[(a.d[0]) & 1]);
+    r.d[1] = sat_add(a.d[1], b.d[(1 + a.d[1]) & 1]);
+    return r;
+}
+
 // |a|^2 as the reference computes it: RN(RN(re*re) + RN(im*im))
 // (measure.cpp:69-70, :141-142).
 QSLC_HD double norm2_rn(double re, double im)

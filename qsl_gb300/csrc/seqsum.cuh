@@ -106,47 +106,104 @@ __global__ void __launch_bounds__(SEQ_TPB) k_seq_tile_sum(Prod pr, uint64_t coun
     }
 }
 
+// Packs a term's grid steps with its tie bit (bit 63); steps never reach
+// 2^62 without also raising `big`.
+constexpr uint64_t TIE_BIT = uint64_t(1) << 63;
+
+__device__ __forceinline__ Tx warp_compose(Tx x)
+{
+    // ordered reduction: after the loop lane 0 holds lane 0 then 1 then ... 31
+    const int lane = threadIdx.x & 31;
+    for (int off = 1; off < 32; off <<= 1) {
+        Tx y;
+        y.d[0] = __shfl_down_sync(0xffffffffu, x.d[0], off);
+        y.d[1] = __shfl_down_sync(0xffffffffu, x.d[1], off);
+        if ((lane & (2 * off - 1)) == 0) x = tx_then(x, y);
+    }
+    return x;
+}
+
+__device__ __forceinline__ Tx warp_scan_incl(Tx x)
+{
+    // inclusive ordered scan: lane l holds lanes 0..l composed in order
+    const int lane = threadIdx.x & 31;
+    for (int off = 1; off < 32; off <<= 1) {
+        Tx y;
+        y.d[0] = __shfl_up_sync(0xffffffffu, x.d[0], off);
+        y.d[1] = __shfl_up_sync(0xffffffffu, x.d[1], off);
+        if (lane >= off) x = tx_then(y, x);
+    }
+    return x;
+}
+
+// Grid steps of every term of a tile into `sm` (coalesced loads), and the
+// OR of the `big` flags.
+template <class Prod, class A>
+__device__ __forceinline__ unsigned tile_terms(const Prod &pr, uint64_t count, uint64_t base, int e,
+                                               uint64_t *sm)
+{
+    unsigned big_any = 0;
+#pragma unroll 4
+    for (int k = 0; k < SEQ_PER; k++) {
+        const int i = k * SEQ_TPB + threadIdx.x;
+        const uint64_t j = base + uint64_t(i);
+        uint64_t v = 0;
+        if (j < count) {
+            bool tie, big;
+            v = grid_steps<A>(A(pr.p(j)), e, tie, big);
+            if (big) {
+                big_any = 1;
+                v = 0;
+            }
+            if (tie) v |= TIE_BIT;
+        }
+        sm[i] = v;
+    }
+    return big_any;
+}
+
+// The transducer of this thread's SEQ_PER consecutive terms of `sm`.
+__device__ __forceinline__ Tx segment_tx(const uint64_t *sm)
+{
+    Tx t = tx_identity();
+#pragma unroll
+    for (int k = 0; k < SEQ_PER; k++) {
+        const uint64_t v = sm[threadIdx.x * SEQ_PER + k];
+        t = tx_then(t, tx_term(v & ~TIE_BIT, (v & TIE_BIT) != 0));
+    }
+    return t;
+}
+
 template <class Prod, class A>
 __global__ void __launch_bounds__(SEQ_TPB) k_seq_tile_steps(Prod pr, uint64_t count, uint64_t ntiles,
                                                             const int16_t *__restrict__ guess,
                                                             uint64_t *__restrict__ steps,
                                                             uint8_t *__restrict__ flags)
 {
-    __shared__ uint64_t red[SEQ_TPB / 32];
-    __shared__ unsigned fl_all;
+    __shared__ uint64_t sm[SEQ_TILE];
+    __shared__ Tx wtx[SEQ_TPB / 32];
+    __shared__ unsigned big_all;
     constexpr uint64_t CAP = uint64_t(1) << (fp_traits<A>::MANT + 1);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (uint64_t b = blockIdx.x; b < ntiles; b += gridDim.x) {
-        if (threadIdx.x == 0) fl_all = 0;
+        if (threadIdx.x == 0) big_all = 0;
         __syncthreads();
-        const int e = guess[b];
-        const uint64_t base = b * SEQ_TILE;
-        uint64_t acc = 0;
-        unsigned fl = 0;
-#pragma unroll 4
-        for (int k = 0; k < SEQ_PER; k++) {
-            uint64_t j = base + uint64_t(k) * SEQ_TPB + threadIdx.x;
-            if (j < count) {
-                bool tie, big;
-                acc += grid_steps<A>(A(pr.p(j)), e, tie, big);
-                fl |= (tie ? 1u : 0u) | (big ? 2u : 0u);
-            }
-        }
-        if (acc >= CAP) {       // saturate: the tile cannot stay in binade e
-            acc = CAP;
-            fl |= 2u;
-        }
-        acc = warp_sum_u(acc);
-        if (fl) atomicOr(&fl_all, fl);
-        if (lane == 0) red[warp] = acc;
+        const unsigned big = tile_terms<Prod, A>(pr, count, b * SEQ_TILE, guess[b], sm);
+        if (big) atomicOr(&big_all, 1u);
         __syncthreads();
-        if (warp == 0) {
-            uint64_t v = lane < SEQ_TPB / 32 ? red[lane] : 0;
-            v = warp_sum_u(v);
-            if (lane == 0) {
-                steps[b] = v;
-                flags[b] = uint8_t(fl_all);
-            }
+        Tx t = segment_tx(sm);
+        // a run of 4096 terms below CAP each stays below 2^62: no overflow
+        t = warp_compose(t);
+        if (lane == 0) wtx[warp] = t;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            Tx tot = wtx[0];
+            for (int w = 1; w < SEQ_TPB / 32; w++) tot = tx_then(tot, wtx[w]);
+            unsigned fl = big_all ? 2u : 0u;
+            if (tot.d[0] >= CAP || tot.d[1] >= CAP) fl |= 2u;
+            steps[2 * b] = tot.d[0] < CAP ? tot.d[0] : CAP;
+            steps[2 * b + 1] = tot.d[1] < CAP ? tot.d[1] : CAP;
+            flags[b] = uint8_t(fl);
         }
         __syncthreads();
     }
@@ -183,45 +240,41 @@ __global__ void __launch_bounds__(SEQ_TPB) k_seq_resolve(Prod pr, uint64_t count
                                                          uint64_t *__restrict__ out_sorted)
 {
     __shared__ uint64_t pre[SEQ_TILE];
-    __shared__ uint64_t wsum[SEQ_TPB / 32];
+    __shared__ Tx wtx[SEQ_TPB / 32];
     constexpr int MANT = fp_traits<A>::MANT;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int q = blockIdx.x; q < nitems; q += gridDim.x) {
         const ResolveItem it = items[q];
         const uint64_t base = it.tile * SEQ_TILE;
-        for (int k = 0; k < SEQ_PER; k++) {
-            int i = k * SEQ_TPB + threadIdx.x;
-            uint64_t j = base + i;
-            uint64_t st = 0;
-            if (j < count) {
-                bool tie, big;
-                st = grid_steps<A>(A(pr.p(j)), it.binade, tie, big);
-            }
-            pre[i] = st;
-        }
-        __syncthreads();
-        // inclusive prefix: each thread owns SEQ_PER consecutive elements
-        uint64_t loc[SEQ_PER];
-        uint64_t run = 0;
-#pragma unroll
-        for (int k = 0; k < SEQ_PER; k++) {
-            run += pre[threadIdx.x * SEQ_PER + k];
-            loc[k] = run;
-        }
-        uint64_t x = run;   // inclusive warp scan of thread totals
-        for (int o = 1; o < 32; o <<= 1) {
-            uint64_t y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        if (lane == 31) wsum[warp] = x;
-        __syncthreads();
-        uint64_t off = x - run;
-        for (int w = 0; w < warp; w++) off += wsum[w];
-#pragma unroll
-        for (int k = 0; k < SEQ_PER; k++) pre[threadIdx.x * SEQ_PER + k] = loc[k] + off;
+        tile_terms<Prod, A>(pr, count, base, it.binade, pre);
         __syncthreads();
         // running sum before the tile, in grid steps of the tile's binade
         const uint64_t s0 = uint64_t(ldexp(it.start, MANT - it.binade));
+        const Tx seg = segment_tx(pre);
+        Tx incl = warp_scan_incl(seg);
+        if (lane == 31) wtx[warp] = incl;
+        __syncthreads();
+        Tx before = tx_identity();                 // warps before this one
+        for (int w = 0; w < warp; w++) before = tx_then(before, wtx[w]);
+        Tx excl_in_warp;
+        excl_in_warp.d[0] = __shfl_up_sync(0xffffffffu, incl.d[0], 1);
+        excl_in_warp.d[1] = __shfl_up_sync(0xffffffffu, incl.d[1], 1);
+        if (lane == 0) excl_in_warp = tx_identity();
+        const Tx prefix = tx_then(before, excl_in_warp);
+        const uint64_t off = prefix.d[s0 & 1];
+        uint64_t loc[SEQ_PER];
+        uint64_t run = off;
+#pragma unroll
+        for (int k = 0; k < SEQ_PER; k++) {
+            const uint64_t v = pre[threadIdx.x * SEQ_PER + k];
+            const Tx t = tx_term(v & ~TIE_BIT, (v & TIE_BIT) != 0);
+            run += t.d[(s0 + run) & 1];
+            loc[k] = run;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < SEQ_PER; k++) pre[threadIdx.x * SEQ_PER + k] = loc[k];
+        __syncthreads();
         for (uint32_t k = threadIdx.x; k < it.nshot; k += SEQ_TPB) {
             const double u = u_sorted[it.shot0 + k];
             int lo = 0, hi = SEQ_TILE - 1;   // first i with partial(i) >= u
@@ -267,7 +320,7 @@ struct SeqScratch {
         char *p = static_cast<char *>(base);
         size_t off = 0;
         s.tile_sum = reinterpret_cast<double *>(p + off); off += align(ntiles * 8);
-        s.steps = reinterpret_cast<uint64_t *>(p + off); off += align(ntiles * 8);
+        s.steps = reinterpret_cast<uint64_t *>(p + off); off += align(ntiles * 16);
         s.guess = reinterpret_cast<int16_t *>(p + off); off += align(ntiles * 2);
         s.flags = reinterpret_cast<uint8_t *>(p + off); off += align(ntiles);
         s.fetch_ids = reinterpret_cast<uint64_t *>(p + off); off += align(size_t(fetch_cap) * 8);
@@ -351,7 +404,7 @@ int seq_core(SeqEnv<P> &env, const Prod &pr, uint64_t count, A *total, A *starts
     k_seq_tile_steps<Prod, A><<<grid, SEQ_TPB, 0, str>>>(pr, count, ntiles, sc.guess, sc.steps, sc.flags);
     (*env.launches)++;
     QSLC_CUDA(cudaGetLastError());
-    QSLC_CUDA(cudaMemcpyAsync(h.steps, sc.steps, ntiles * 8, cudaMemcpyDeviceToHost, str));
+    QSLC_CUDA(cudaMemcpyAsync(h.steps, sc.steps, ntiles * 16, cudaMemcpyDeviceToHost, str));
     QSLC_CUDA(cudaMemcpyAsync(h.flags, sc.flags, ntiles, cudaMemcpyDeviceToHost, str));
     QSLC_CUDA(cudaStreamSynchronize(str));
 
@@ -391,10 +444,11 @@ int seq_core(SeqEnv<P> &env, const Prod &pr, uint64_t count, A *total, A *starts
         const int e = h.guess[b];
         bool ok = h.flags[b] == 0 && sum > A(0) && binade<A>(sum) == e && e >= T::EMIN;
         if (ok) {
-            uint64_t s0 = uint64_t(std::ldexp(double(sum), T::MANT - e));
-            ok = s0 + h.steps[b] < cap;
+            const uint64_t s0 = uint64_t(std::ldexp(double(sum), T::MANT - e));
+            const uint64_t d = h.steps[2 * b + (s0 & 1)];   // ties round to even
+            ok = s0 + d < cap;
             if (ok) {
-                sum = grid_value<A>(s0 + h.steps[b], e);
+                sum = grid_value<A>(s0 + d, e);
                 continue;
             }
         }
@@ -426,7 +480,7 @@ int seq_run(qslc_state *s, const Prod &pr, uint64_t count, bool keep_partials, S
     int rc = s->scratch.ensure(probe.bytes);
     if (rc) return rc;
     std::vector<double> est(ntiles);
-    std::vector<uint64_t> steps(ntiles), slot_tile(cap), batch(cap);
+    std::vector<uint64_t> steps(2 * ntiles), slot_tile(cap), batch(cap);
     std::vector<uint8_t> flags(ntiles), predicted(ntiles);
     out.guess.assign(ntiles, 0);
     std::vector<P> slot_terms(size_t(cap) * SEQ_TILE);

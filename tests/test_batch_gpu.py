@@ -1,0 +1,48 @@
+"""The batching form against the oracle, instance by instance: every
+circuit's probabilities and shots are the bits the reference's Default
+backend gives for the same gate calls and uniforms, in complex128 and in
+complex64, for states in shared memory and states in the global arena."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def reference_instance(port, n, layers, angles, u, fp32):
+    sim = port.PortQubits(n, fp32=fp32)
+    a = angles.reshape(layers, n, 2)
+    for l in range(layers):
+        for q in range(n):
+            sim.gate("rotateY", q, None, a[l, q, 0])
+        for q in range(n):
+            sim.gate("rotateZ", q, None, a[l, q, 1])
+        for q in range(n - 1):
+            sim.gate("controlNot", q, q + 1)
+    probs = np.array([[sim.prob(q, 0), sim.prob(q, 1)] for q in range(n)])
+    return probs, sim.sample_all(u)
+
+
+@pytest.mark.parametrize("dtype", [np.complex128, np.complex64])
+def test_batch_matches_oracle(qsl, port, dtype):
+    rng = np.random.default_rng(11)
+    ns = np.array([2, 5, 10, 13, 14, 15, 16, 12, 3, 11], dtype=np.uint32)
+    ls = rng.integers(1, 6, ns.size).astype(np.uint32)
+    nshots = 257
+    b = qsl.Batch(ns, ls, nshots, dtype=dtype)
+    angles = rng.uniform(0, 2 * np.pi, b.angle_count)
+    fp32 = dtype == np.complex64
+    if fp32:
+        angles = angles.astype(np.float32).astype(np.float64)
+    u = rng.random(ns.size * nshots)
+    if fp32:
+        u = u.astype(np.float32).astype(np.float64)
+    for rep in range(2):                 # the graph replays
+        probs, shots = b.run(angles, u)
+        at = 0
+        for i, (n, L) in enumerate(zip(ns, ls)):
+            cnt = 2 * int(n) * int(L)
+            p, sh = reference_instance(port, int(n), int(L), angles[at:at + cnt],
+                                       u[i * nshots:(i + 1) * nshots], fp32)
+            at += cnt
+            assert np.array_equal(probs[i], p), (rep, i, n)
+            assert np.array_equal(shots[i], sh), (rep, i, n)
