@@ -74,6 +74,13 @@ def kernel_of(gate: str) -> str:
             "controlPhase": "k_diag2<PHASE>"}[gate]
 
 
+# DRAM bytes per launch over algorithmic bytes for the dense one-qubit
+# kernels, from the ncu capture summarised in
+# profiles/k_pair1_dense_gates_26q.md (2.092 GB moved for 2.147 GB of
+# algorithmic traffic at 26 qubits; it scales with the amplitude count).
+K_PAIR1_TRAFFIC_RATIO = 2.092 / 2.147
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -157,26 +164,32 @@ def run_fused(args, torch, q, stream):
     """The precision form (fused FP32 blocks, FP64 norms and CDF): the layered
     circuit at depth 60 on a 32-qubit complex64 state, k = 5, against the
     plain FP64 path at the same size; infidelity on a 28-qubit instance."""
-    n, depth, k = args.fused_qubits, 60, 5
+    n, depth = args.fused_qubits, 60
     circ = workloads.layered_mixed(n, depth, SEED + 4)
     per = n + n // 2
     warm, timed = circ[:3 * per], circ[3 * per:]
-    sim = q.Qubits(n, dtype=np.complex64)
-    sim.set_stream(stream.cuda_stream)
-    sim.set_fusion(k)
-    workloads.apply(sim, warm)
-    sim.flush()
-    torch.cuda.synchronize()
-    b0 = sim.fused_blocks()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    workloads.apply(sim, timed)
-    sim.flush()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    fused_ms = e0.elapsed_time(e1)
-    blocks = sim.fused_blocks() - b0
+    by_k = {}
+    for kk in (4, 5):
+        sim = q.Qubits(n, dtype=np.complex64)
+        sim.set_stream(stream.cuda_stream)
+        sim.set_fusion(kk)
+        workloads.apply(sim, warm)
+        sim.flush()
+        torch.cuda.synchronize()
+        b0 = sim.fused_blocks()
+        e0.record(stream)
+        workloads.apply(sim, timed)
+        sim.flush()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        by_k[kk] = {"ms": e0.elapsed_time(e1), "blocks": sim.fused_blocks() - b0}
+        if kk != 5:
+            del sim
+            torch.cuda.empty_cache()
+    k = min(by_k, key=lambda kk: by_k[kk]["ms"])
+    fused_ms, blocks = by_k[k]["ms"], by_k[k]["blocks"]
     su = workloads.uniforms(args.shots, SEED + 5)
     t0 = time.perf_counter()
     sim.sample_shots(su)
@@ -210,6 +223,9 @@ def run_fused(args, torch, q, stream):
     del ref, f, a, b
     fused_gps = len(timed) / (fused_ms * 1e-3)
     return {"nqubits": n, "dtype": "c64 state, FP32 blocks, FP64 norms/CDF", "k": k,
+            "by_k": {str(kk): {"ms": v["ms"], "blocks": v["blocks"],
+                               "equivalent_gates_per_s": len(timed) / (v["ms"] * 1e-3)}
+                     for kk, v in by_k.items()},
             "depth": depth, "gates_timed": len(timed), "fused_blocks": blocks,
             "gates_per_block": len(timed) / max(blocks, 1), "ms": fused_ms,
             "equivalent_gates_per_s": fused_gps,
@@ -259,6 +275,64 @@ def run_np(args, torch, q, stream):
                 break
         out["cpu_baseline"] = {"value": done / (time.perf_counter() - t0), "unit": UNIT, "cores": thr,
                                "kind": "port", "sample": f"first {done} gates, OpenMP NP restatement"}
+    return out
+
+
+def run_batch(args, torch, q):
+    """The batching form: 4096 independent ansatz circuits, n uniform in
+    [10, 20], L uniform in [4, 16] layers of rotateY/rotateZ on every qubit
+    plus a controlNot ladder, per-instance angles; every qubit's
+    probabilities and 1024 shots per instance; one persistent launch from a
+    CUDA graph, complex64 and complex128.  The plain FP64 path (per-gate
+    launches through the C ABI) runs a random subset of the same instances."""
+    rng = np.random.default_rng(SEED + 8)
+    ninst, nshots = args.batch_instances, 1024
+    ns = rng.integers(10, 21, ninst).astype(np.uint32)
+    ls = rng.integers(4, 17, ninst).astype(np.uint32)
+    gates = ls.astype(np.int64) * (3 * ns.astype(np.int64) - 1)
+    total_gates = int(gates.sum())
+    angles = rng.uniform(0, 2 * np.pi, int(np.sum(2 * ns.astype(np.int64) * ls)))
+    u = workloads.uniforms(ninst * nshots, SEED + 9)
+    out = {"instances": ninst, "shots_per_instance": nshots, "total_gates": total_gates,
+           "state_bytes_c128": int(np.sum((1 << ns.astype(np.int64)) * 16))}
+    for name, dt in (("c64", np.complex64), ("c128", np.complex128)):
+        b = q.Batch(ns, ls, nshots, dtype=dt)
+        b.run(angles, u)                                  # warm-up replay
+        reps = 2
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            b.run(angles, u)
+        dt_s = (time.perf_counter() - t0) / reps
+        out[name] = {"s": dt_s, "gates_per_s": total_gates / dt_s}
+        del b
+    # plain FP64 path on a random subset, scaled by gate count
+    sub = rng.choice(ninst, args.batch_plain_sample, replace=False)
+    at = np.concatenate([[0], np.cumsum(2 * ns.astype(np.int64) * ls)])
+    t0 = time.perf_counter()
+    g = 0
+    for i in sub:
+        n, L = int(ns[i]), int(ls[i])
+        a = angles[at[i]:at[i + 1]].reshape(L, n, 2)
+        sim = q.Qubits(n)
+        for l in range(L):
+            for qq in range(n):
+                sim.rotateY(qq, a[l, qq, 0])
+            for qq in range(n):
+                sim.rotateZ(qq, a[l, qq, 1])
+            for qq in range(n - 1):
+                sim.controlNot(qq, qq + 1)
+        for qq in range(n):
+            sim.prob(qq, 0)
+            sim.prob(qq, 1)
+        sim.sample_shots(u[i * nshots:(i + 1) * nshots])
+        g += int(gates[i])
+        del sim
+    plain_s = time.perf_counter() - t0
+    plain_gps = g / plain_s
+    out["plain_fp64_gates_per_s"] = plain_gps
+    out["plain_sample_instances"] = int(args.batch_plain_sample)
+    out["speedup_c64_vs_plain_fp64"] = out["c64"]["gates_per_s"] / plain_gps
+    out["speedup_c128_vs_plain_fp64"] = out["c128"]["gates_per_s"] / plain_gps
     return out
 
 
@@ -393,7 +467,13 @@ def run_gpu(args):
         },
         "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": args.traffic},
+                     "traffic": args.traffic if args.traffic else (
+                         top["bytes"] / top["launches"] * K_PAIR1_TRAFFIC_RATIO
+                         if top_name.startswith("k_pair1") else None),
+                     "traffic_source": "ncu dram__bytes_read+write of k_pair1 at 26 qubits, "
+                                       "scaled by amplitudes (profiles/k_pair1_dense_gates_26q.md)",
+                     "limiter": "FP64 pipe (83% active in ncu): the reference's rounding costs "
+                                "12 FP64 operations per amplitude pair"},
         "gpu_launches": launches,
         "clocks": clk,
     }
@@ -405,6 +485,8 @@ def run_gpu(args):
         line["fused"] = run_fused(args, torch, q, stream)
     if not args.no_np:
         line["np"] = run_np(args, torch, q, stream)
+    if not args.no_batch:
+        line["batch"] = run_batch(args, torch, q)
     if rank == 0 and not args.no_cpu:
         v, done, thr = cpu_sample(circ, n, seconds=args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": thr, "kind": "port",
@@ -474,6 +556,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fused", action="store_true")
     ap.add_argument("--no-np", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-instances", type=int, default=4096)
+    ap.add_argument("--batch-plain-sample", type=int, default=48)
     ap.add_argument("--fused-qubits", type=int, default=32)
     ap.add_argument("--fused-check-qubits", type=int, default=28)
     ap.add_argument("--traffic", type=float, default=None,

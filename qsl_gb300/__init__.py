@@ -71,6 +71,7 @@ SIGNATURES = {
                                     C.POINTER(C.c_double)]),
     "qslc_set_fusion": (C.c_int, [_VP, C.c_uint]),
     "qslc_flush": (C.c_int, [_VP]),
+    "qslc_set_fusion_tc": (C.c_int, [_VP, C.c_int]),
     "qslc_fused_blocks": (C.c_uint64, [_VP]),
     "qslc_batch_create": (C.c_int, [C.c_int, C.c_uint32, _VP, _VP, C.c_uint32,
                                     C.POINTER(C.c_void_p)]),
@@ -228,6 +229,10 @@ class Qubits:
 
     def flush(self) -> None:
         _check(self.L.qslc_flush(self.h))
+
+    def set_fusion_tc(self, on: bool) -> None:
+        """Apply five-qubit fused blocks on the tensor cores (tcgen05)."""
+        _check(self.L.qslc_set_fusion_tc(self.h, int(on)))
 
     def fused_blocks(self) -> int:
         return int(self.L.qslc_fused_blocks(self.h))

@@ -141,6 +141,7 @@ void free_state(qslc_state *s)
     s->scratch.release();
     s->scratch2.release();
     s->fuse_mats.release();
+    s->fuse_tc_mats.release();
     if (s->host_pinned) cudaFreeHost(s->host_pinned);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
     delete s;
@@ -575,6 +576,15 @@ int qslc_set_fusion(qslc_state *s, unsigned max_qubits)
     rc = flushed(s);
     if (rc) return rc;
     s->fuse_k = max_qubits;
+    return QSLC_OK;
+}
+
+int qslc_set_fusion_tc(qslc_state *s, int on)
+{
+    int rc = check_handle(s);
+    if (!rc) rc = flushed(s);
+    if (rc) return rc;
+    s->fuse_tc = on ? 1 : 0;
     return QSLC_OK;
 }
 

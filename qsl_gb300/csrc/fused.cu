@@ -98,9 +98,38 @@ int fusion_flush(qslc_state *s)
     if (rc) return rc;
     float2 *d = static_cast<float2 *>(s->fuse_mats.ptr);
     QSLC_CUDA(cudaMemcpyAsync(d, mats.data(), total * sizeof(float2), cudaMemcpyHostToDevice, s->stream));
+    // five-qubit blocks for the tensor cores: their real-form operands, split
+    const bool tc = s->fuse_tc && tc_usable(s);
+    float *d_tc = nullptr;
+    int *d_err = nullptr;
+    std::vector<float> packed;
+    if (tc) {
+        size_t n5 = 0;
+        for (const Block &b : blocks) n5 += b.k == 5;
+        const size_t per = tc_block_floats();
+        packed.resize(n5 * per + 4);
+        size_t i5 = 0;
+        for (const Block &b : blocks)
+            if (b.k == 5) tc_pack_block(b.U, packed.data() + per * i5++);
+        rc = s->fuse_tc_mats.ensure(packed.size() * sizeof(float));
+        if (rc) return rc;
+        d_tc = static_cast<float *>(s->fuse_tc_mats.ptr);
+        d_err = reinterpret_cast<int *>(d_tc + n5 * per);
+        QSLC_CUDA(cudaMemcpyAsync(d_tc, packed.data(), packed.size() * sizeof(float), cudaMemcpyHostToDevice,
+                                  s->stream));
+        QSLC_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int), s->stream));
+    }
     at = 0;
+    size_t i5 = 0;
     for (const Block &b : blocks) {
         const float2 *U = d + at;
+        if (tc && b.k == 5) {
+            rc = tc_launch(s, d_tc + tc_block_floats() * i5++, b.qubits, d_err);
+            if (rc) return rc;
+            at += size_t(1) << (2 * b.k);
+            s->fused_blocks++;
+            continue;
+        }
         switch (b.k) {
         case 1: launch_dense<1>(s, U, b.qubits); break;
         case 2: launch_dense<2>(s, U, b.qubits); break;
@@ -113,6 +142,12 @@ int fusion_flush(qslc_state *s)
     }
     // a copy from pageable memory has left `mats` once cudaMemcpyAsync returns
     QSLC_CUDA(cudaGetLastError());
+    if (tc) {
+        int err = 0;
+        QSLC_CUDA(cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+        QSLC_CUDA(cudaStreamSynchronize(s->stream));
+        if (err) return fail(QSLC_ETIMEOUT, "a tensor-core block did not complete in time");
+    }
     return QSLC_OK;
 }
 

@@ -111,8 +111,10 @@ struct qslc_state {
     qslc::NPTables *npt = nullptr;
     // precision form (fused.cu): queued gates, fusion width, block matrices
     unsigned fuse_k = 0;
+    int fuse_tc = 0;          // five-qubit blocks on the tensor cores (fused_tc.cu)
     std::vector<qslc::GateOp> fuse_queue;
     qslc::Scratch fuse_mats;
+    qslc::Scratch fuse_tc_mats;   // packed tensor-core operands, then an error word
     uint64_t fused_blocks = 0;
 
     size_t amp_bytes() const { return dtype == QSLC_C128 ? 16 : 8; }
@@ -144,6 +146,12 @@ int launch_fill_basis(qslc_state *s, uint64_t pos);
 
 // fused.cu
 int fusion_flush(qslc_state *s);
+
+// fused_tc.cu
+void tc_pack_block(const std::vector<cd> &U, float *out);
+size_t tc_block_floats();
+bool tc_usable(const qslc_state *s);
+int tc_launch(qslc_state *s, const float *d_b, const unsigned *pos, int *d_err);
 
 // measure.cu
 int seq_prob(qslc_state *s, unsigned targ, unsigned outcome, double *out);
