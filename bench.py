@@ -171,10 +171,11 @@ def run_fused(args, torch, q, stream):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     by_k = {}
-    for kk in (4, 5):
+    for kk in (4, 5, "5tc"):
         sim = q.Qubits(n, dtype=np.complex64)
         sim.set_stream(stream.cuda_stream)
-        sim.set_fusion(kk)
+        sim.set_fusion(5 if kk == "5tc" else kk)
+        sim.set_fusion_tc(kk == "5tc")
         workloads.apply(sim, warm)
         sim.flush()
         torch.cuda.synchronize()
@@ -185,7 +186,7 @@ def run_fused(args, torch, q, stream):
         e1.record(stream)
         torch.cuda.synchronize()
         by_k[kk] = {"ms": e0.elapsed_time(e1), "blocks": sim.fused_blocks() - b0}
-        if kk != 5:
+        if kk != "5tc":
             del sim
             torch.cuda.empty_cache()
     k = min(by_k, key=lambda kk: by_k[kk]["ms"])
@@ -214,7 +215,8 @@ def run_fused(args, torch, q, stream):
     ref = q.Qubits(m)
     workloads.apply(ref, c28)
     f = q.Qubits(m, dtype=np.complex64)
-    f.set_fusion(k)
+    f.set_fusion(5 if k == "5tc" else k)
+    f.set_fusion_tc(k == "5tc")
     workloads.apply(f, c28)
     a = ref.getState()
     b = f.getState().astype(np.complex128)
@@ -222,7 +224,8 @@ def run_fused(args, torch, q, stream):
     maxerr = float(np.abs(a - b).max())
     del ref, f, a, b
     fused_gps = len(timed) / (fused_ms * 1e-3)
-    return {"nqubits": n, "dtype": "c64 state, FP32 blocks, FP64 norms/CDF", "k": k,
+    return {"nqubits": n, "dtype": "c64 state, FP32 blocks (tensor cores: 3xTF32 tcgen05), "
+                                   "FP64 norms/CDF", "k": k,
             "by_k": {str(kk): {"ms": v["ms"], "blocks": v["blocks"],
                                "equivalent_gates_per_s": len(timed) / (v["ms"] * 1e-3)}
                      for kk, v in by_k.items()},

@@ -189,6 +189,35 @@ public:
         return results;
     }
 
+    /// sampleAll2 (measure.cpp:237-267): every basis index is a key of the
+    /// result (np/measure.cpp:259-289: every index of the preserved weight).
+    std::map<std::size_t, std::size_t> sampleAll2(std::size_t nsamples)
+    {
+        std::vector<double> u(nsamples);
+        for (auto &x : u) x = double(draw());
+        std::vector<std::uint64_t> bins(nsamples);
+        check(qslc_sample_all2(h, u.data(), u.size(), bins.data()));
+        std::map<std::size_t, std::size_t> results;
+        const unsigned n = getNumQubits();
+        if (qslc_is_np(h)) {
+            unsigned w = 0;
+            check(qslc_num_ones(h, &w));
+            std::uint64_t x = (std::uint64_t(1) << w) - 1;
+            const std::uint64_t end = x << (n - w);
+            while (true) {
+                results[std::size_t(x)] = 0;
+                if (x == end) break;
+                const std::uint64_t t = x | (x - 1);
+                x = (t + 1) | (((~t & (t + 1)) - 1) >> (__builtin_ctzll(x) + 1));
+            }
+        } else {
+            for (std::size_t i = 0; i < (std::size_t(1) << n); i++) results[i] = 0;
+        }
+        for (auto b : bins)
+            if (b != ~std::uint64_t(0)) results[std::size_t(b)]++;
+        return results;
+    }
+
     // Gates every backend has (HasNPGates, concepts.hpp:65-82) ---------
     void pauliZ(unsigned targ) { gate1(QSLC_PAULI_Z, targ); }
     void rotateZ(unsigned targ, Fp angle) { gate1(QSLC_ROTATE_Z, targ, angle); }

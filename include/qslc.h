@@ -173,6 +173,15 @@ QSLC_API int qslc_sample(qslc_state *s, unsigned targ, const double *u, uint64_t
  * reference folds these into a std::map of counts. */
 QSLC_API int qslc_sample_all(qslc_state *s, const double *u, uint64_t nshots, uint64_t *out);
 
+/* sampleAll2(nsamples) (measure.cpp:237-267; np/measure.cpp:259-289): the
+ * bin each uniform falls in under the reference's merge of sorted uniforms
+ * against an Fp running sum -- the first basis index whose running sum
+ * exceeds u -- into out[0..nshots), in the order of u.  A uniform at or
+ * above the total falls in no bin (the reference counts it nowhere) and
+ * reads back as UINT64_MAX.  The reference returns a std::map with every
+ * index as a key; count the outcomes to rebuild it. */
+QSLC_API int qslc_sample_all2(qslc_state *s, const double *u, uint64_t nshots, uint64_t *out);
+
 /* measureAll (measure.cpp:110-123): draw one index with `u`, then collapse
  * to that basis state. */
 QSLC_API int qslc_measure_all(qslc_state *s, double u, uint64_t *outcome);

@@ -105,6 +105,7 @@ def port_lib():
             sig("np_prob", fp, vp, vp, C.c_size_t, C.c_uint, C.c_uint)
             sig("np_collapse", None, vp, vp, C.c_size_t, vp, C.c_size_t, C.c_uint, C.c_uint, fp)
             sig("np_generate_dist", C.c_size_t, vp, vp, C.c_size_t, vp, vp)
+            sig("np_sample_all2", None, vp, vp, C.c_size_t, vp, C.c_size_t, vp)
         lib.port_next.restype = C.c_uint64
         lib.port_next.argtypes = [C.c_uint64]
         lib.port_hamming_weight.restype = C.c_uint
@@ -322,6 +323,14 @@ class PortNPQubits:
         idx, cdf = self.dist()
         f = self._f("draw_sample")
         return np.array([f(_ptr(idx), _ptr(cdf), idx.size, x) for x in u], dtype=np.uint64)
+
+    def sample_all2(self, uniforms) -> np.ndarray:
+        """counts per weight-w basis index (table {n, w} order)"""
+        u = np.sort(np.ascontiguousarray(uniforms, dtype=self.rdtype))
+        t, m = self._t(self.n, self.w)
+        counts = np.zeros(m, dtype=np.uint64)
+        self._f("np_sample_all2")(_ptr(self.state), t, m, _ptr(u), u.size, _ptr(counts))
+        return counts
 
     def measure_all(self, u: float) -> int:
         out = int(self.sample_all([u])[0])

@@ -66,7 +66,10 @@ enum {
                                   unsigned targ, unsigned o, FP factor);      \
     size_t port_##SFX##_np_generate_dist(const FP *s, const uint64_t *tab,    \
                                          size_t len, uint64_t *idx,           \
-                                         double *cdf);
+                                         double *cdf);                        \
+    void port_##SFX##_np_sample_all2(const FP *s, const uint64_t *tab,        \
+                                     size_t len, const FP *u_sorted,          \
+                                     size_t nshots, uint64_t *counts);
 
 PORT_DECL(double, d)
 PORT_DECL(float, f)

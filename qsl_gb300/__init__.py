@@ -63,6 +63,7 @@ SIGNATURES = {
     "qslc_sample": (C.c_int, [_VP, C.c_uint, _VP, C.c_uint64, _VP]),
     "qslc_sample_all": (C.c_int, [_VP, _VP, C.c_uint64, _VP]),
     "qslc_measure_all": (C.c_int, [_VP, C.c_double, C.POINTER(C.c_uint64)]),
+    "qslc_sample_all2": (C.c_int, [_VP, _VP, C.c_uint64, _VP]),
     "qslc_set_stream": (C.c_int, [_VP, _VP]),
     "qslc_get_stream": (C.c_void_p, [_VP]),
     "qslc_synchronize": (C.c_int, [_VP]),
@@ -275,6 +276,28 @@ class Qubits:
         keys, counts = np.unique(shots, return_counts=True)
         return {int(k): int(c) for k, c in zip(keys, counts)}
 
+    def sample_shots2(self, uniforms) -> np.ndarray:
+        """Bins under sampleAll2's rule; 2**64-1 for a uniform counted nowhere."""
+        u = np.ascontiguousarray(uniforms, dtype=np.float64)
+        out = np.empty(u.size, dtype=np.uint64)
+        _check(self.L.qslc_sample_all2(self.h, _ptr(u), u.size, _ptr(out)))
+        return out
+
+    def sampleAll2(self, nsamples: int, uniforms=None) -> dict:
+        """sampleAll2: counts for every basis index (zeros included), as qsl returns."""
+        u = self.rng.random(nsamples) if uniforms is None else uniforms
+        shots = self.sample_shots2(u)
+        shots = shots[shots != np.uint64(2**64 - 1)]
+        keys = self._basis_keys()
+        counts = dict.fromkeys((int(k) for k in keys), 0)
+        k, c = np.unique(shots, return_counts=True)
+        for a, b in zip(k, c):
+            counts[int(a)] = int(b)
+        return counts
+
+    def _basis_keys(self):
+        return np.arange(1 << self.nqubits, dtype=np.uint64)
+
     def sample(self, targ: int, nsamples: int, uniforms=None) -> list:
         u = np.ascontiguousarray(self.rng.random(nsamples) if uniforms is None else uniforms,
                                  dtype=np.float64)
@@ -329,6 +352,10 @@ class QubitsNP(Qubits):
 
     def num_stored(self) -> int:
         return int(self.L.qslc_num_stored(self.h))
+
+    def _basis_keys(self):
+        from .workloads import weight_indices
+        return weight_indices(self.nqubits, self.getNumOnes()).astype(np.uint64)
 
 
 class Batch:

@@ -523,6 +523,25 @@ int qslc_sample_all(qslc_state *s, const double *u, uint64_t nshots, uint64_t *o
     return s->np ? np_sample_all(s, u, nshots, out) : seq_sample_all(s, u, nshots, out);
 }
 
+int qslc_sample_all2(qslc_state *s, const double *u, uint64_t nshots, uint64_t *out)
+{
+    int rc = check_handle(s);
+    if (rc) return rc;
+    if (nshots == 0) return QSLC_OK;
+    if (!u || !out) return fail(QSLC_EINVAL, "null pointer");
+    if (nshots > 0xFFFFFFFFull) return fail(QSLC_EINVAL, "at most 2^32-1 shots per call");
+    rc = flushed(s);
+    if (rc) return rc;
+    std::vector<double> uf;
+    const double *uu = u;
+    if (s->dtype == QSLC_C64) {     // Fp uniforms, as the reference draws them (:243)
+        uf.resize(nshots);
+        for (uint64_t i = 0; i < nshots; i++) uf[i] = double(float(u[i]));
+        uu = uf.data();
+    }
+    return s->np ? np_sample_all2(s, uu, nshots, out) : seq_sample_all2(s, uu, nshots, out);
+}
+
 int qslc_measure_all(qslc_state *s, double u, uint64_t *outcome)
 {
     uint64_t o = 0;

@@ -39,6 +39,21 @@ static int sample_all_t(qslc_state *s, const double *u, uint64_t n, uint64_t *ou
     return seq_sample<ProdAll<T>, T, double>(s, pr, uint64_t(1) << s->n, u, n, out, host_index);
 }
 
+// sampleAll2 (measure.cpp:237-267): an Fp running sum, strict comparison
+template <class T>
+static int sample_all2_t(qslc_state *s, const double *u, uint64_t n, uint64_t *out)
+{
+    ProdAll<T> pr{static_cast<const cplx<T> *>(s->amps)};
+    auto host_index = [](uint64_t j) { return j; };
+    return seq_sample<ProdAll<T>, T, T>(s, pr, uint64_t(1) << s->n, u, n, out, host_index, true);
+}
+
+int seq_sample_all2(qslc_state *s, const double *u, uint64_t n, uint64_t *out)
+{
+    return s->dtype == QSLC_C128 ? sample_all2_t<double>(s, u, n, out)
+                                 : sample_all2_t<float>(s, u, n, out);
+}
+
 int seq_sample_all(qslc_state *s, const double *u, uint64_t n, uint64_t *out)
 {
     return s->dtype == QSLC_C128 ? sample_all_t<double>(s, u, n, out)

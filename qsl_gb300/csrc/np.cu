@@ -472,6 +472,23 @@ static int np_sample_t(qslc_state *s, const double *u, uint64_t n, uint64_t *out
     return seq_sample<ProdNPAll<T>, T, T>(s, pr, s->namps, u, n, out, host_index);
 }
 
+// sampleAll2 over the weight-w sector (np/measure.cpp:259-289)
+template <class T>
+static int np_sample2_t(qslc_state *s, const double *u, uint64_t n, uint64_t *out)
+{
+    NPTables *tb = tables_of(s);
+    ProdNPAll<T> pr{static_cast<const cplx<T> *>(s->amps), tb->tab[T_NW]};
+    const unsigned w = s->nones, nq = s->n;
+    auto host_index = [nq, w](uint64_t j) -> uint64_t { return unrank_of(j, nq, w); };
+    return seq_sample<ProdNPAll<T>, T, T>(s, pr, s->namps, u, n, out, host_index, true);
+}
+
+int np_sample_all2(qslc_state *s, const double *u, uint64_t n, uint64_t *out)
+{
+    return s->dtype == QSLC_C128 ? np_sample2_t<double>(s, u, n, out)
+                                 : np_sample2_t<float>(s, u, n, out);
+}
+
 int np_sample_all(qslc_state *s, const double *u, uint64_t n, uint64_t *out)
 {
     return s->dtype == QSLC_C128 ? np_sample_t<double>(s, u, n, out)

@@ -156,6 +156,7 @@ int tc_launch(qslc_state *s, const float *d_b, const unsigned *pos, int *d_err);
 // measure.cu
 int seq_prob(qslc_state *s, unsigned targ, unsigned outcome, double *out);
 int seq_sample_all(qslc_state *s, const double *u_host, uint64_t nshots, uint64_t *out_host);
+int seq_sample_all2(qslc_state *s, const double *u_host, uint64_t nshots, uint64_t *out_host);
 
 // np.cu
 int np_init_tables();
@@ -165,6 +166,7 @@ int np_gate(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle);
 int np_collapse(qslc_state *s, unsigned targ, unsigned outcome, double factor);
 int np_prob(qslc_state *s, unsigned targ, unsigned outcome, double *out);
 int np_sample_all(qslc_state *s, const double *u, uint64_t n, uint64_t *out);
+int np_sample_all2(qslc_state *s, const double *u, uint64_t n, uint64_t *out);
 int np_expand(qslc_state *s, void *host_full);
 int np_compress(qslc_state *s, const void *host_full, unsigned w);
 uint64_t np_choose(unsigned n, unsigned k);

@@ -229,7 +229,7 @@ struct ResolveItem {
     int32_t binade;     // binade the sum stays in throughout the tile
     uint32_t shot0;     // first shot (index into the sorted uniforms)
     uint32_t nshot;
-    uint32_t pad;
+    uint32_t strict;    // 1: first partial sum > u (sampleAll2); 0: >= u (sampleAll)
 };
 
 template <class Prod, class A>
@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(SEQ_TPB) k_seq_resolve(Prod pr, uint64_t count
             while (lo < hi) {
                 int mid = (lo + hi) >> 1;
                 double v = double(A(ldexp(double(s0 + pre[mid]), it.binade - MANT)));
-                if (v >= u) hi = mid;
+                if (it.strict ? (v > u) : (v >= u)) hi = mid;
                 else lo = mid + 1;
             }
             const uint64_t last = count - 1 - base;   // the tile's last valid element
@@ -508,9 +508,13 @@ int seq_run(qslc_state *s, const Prod &pr, uint64_t count, bool keep_partials, S
 // Sampling: for each uniform, the element whose partial sum is the first to
 // reach it.  `host_index` maps an element to its basis index for shots that
 // land in replayed tiles.  Outcomes go to out[0..n) in the order of u.
+// strict (sampleAll2, measure.cpp:237-267): the first element whose
+// partial sum exceeds u; a uniform at or above the total lands nowhere and
+// is reported as ~0.  Otherwise (sampleAll): the first partial sum >= u,
+// and 0 above the total.
 template <class Prod, class P, class A, class HostIndex>
 int seq_sample(qslc_state *s, const Prod &pr, uint64_t count, const double *u, uint64_t n,
-               uint64_t *out, HostIndex host_index)
+               uint64_t *out, HostIndex host_index, bool strict = false)
 {
     SeqOut<A> so;
     int rc = seq_run<Prod, P, A>(s, pr, count, true, so);
@@ -528,26 +532,29 @@ int seq_sample(qslc_state *s, const Prod &pr, uint64_t count, const double *u, u
     uint64_t b = 0;
     for (uint64_t k = 0; k < n;) {
         const double uk = us[k];
-        if (uk > double(so.total)) {   // past the total: the reference returns 0 (:167)
-            res[k++] = 0;
+        const uint64_t none = strict ? ~uint64_t(0) : 0;
+        auto reaches = [strict](double v, double x) { return strict ? v > x : v >= x; };
+        if (!reaches(double(so.total), uk)) {   // past the total (:167, :258)
+            res[k++] = none;
             continue;
         }
         // first tile whose end reaches uk
         while (b < ntiles) {
             double end = (b + 1 < ntiles) ? double(so.starts[b + 1]) : double(so.total);
-            if (end >= uk) break;
+            if (reaches(end, uk)) break;
             b++;
         }
-        if (b >= ntiles) { res[k++] = 0; continue; }
+        if (b >= ntiles) { res[k++] = none; continue; }
         const double end = (b + 1 < ntiles) ? double(so.starts[b + 1]) : double(so.total);
         uint64_t k1 = k;
-        while (k1 < n && us[k1] <= end) k1++;
+        while (k1 < n && reaches(end, us[k1])) k1++;
         auto pit = so.partials.find(b);
         if (pit != so.partials.end()) {
             const std::vector<A> &part = pit->second;
             for (uint64_t q = k; q < k1; q++) {
-                uint64_t i = uint64_t(std::lower_bound(part.begin(), part.end(), us[q],
-                                                       [](A v, double x) { return double(v) < x; }) -
+                const double x = us[q];
+                uint64_t i = uint64_t(std::find_if(part.begin(), part.end(),
+                                                   [&](A v) { return reaches(double(v), x); }) -
                                       part.begin());
                 if (i >= SEQ_TILE) i = SEQ_TILE - 1;
                 res[q] = host_index(b * SEQ_TILE + i);
@@ -559,6 +566,7 @@ int seq_sample(qslc_state *s, const Prod &pr, uint64_t count, const double *u, u
             it.binade = so.guess[b];
             it.shot0 = uint32_t(k);
             it.nshot = uint32_t(k1 - k);
+            it.strict = strict ? 1u : 0u;
             items.push_back(it);
             for (uint64_t q = k; q < k1; q++) on_device[q] = 1;
         }

@@ -91,6 +91,10 @@ def case_default(seed, n, fp32):
     probs = np.array([[ref.prob(t, o) for o in (0, 1)] for t in range(n)])
     u = uniforms(rng, 2000, fp32)
     keys, counts = feed_map(ref, u)
+    u2 = uniforms(rng, 1500, fp32)
+    oracle.ref_feed_uniforms(u2)
+    m2 = ref.sample_all2(len(u2))
+    counts2 = np.array([m2[i] for i in range(1 << n)], dtype=np.uint64)
     mu = uniforms(rng, 4, fp32)
     mq = rng.choice(n, 4, replace=False).astype(np.int32)
     outs = []
@@ -98,6 +102,7 @@ def case_default(seed, n, fp32):
         oracle.ref_feed_uniforms([x])
         outs.append(ref.measure(int(q)))
     return dict(init=init, final=final, probs=probs, u=u, keys=keys, counts=counts,
+                u2=u2, counts2=counts2,
                 measure_qubits=mq, measure_u=mu, measure_out=np.array(outs, dtype=np.int32),
                 after_measure=ref.get_state(), **dict(zip(("names", "q1", "q2", "ang"), encode(circ))))
 

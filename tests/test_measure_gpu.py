@@ -98,3 +98,37 @@ def test_adversarial_sums(qsl, port):
         total = cpu.dist()[1][-1] if cpu.dist()[1].size else 0.0
         u = np.concatenate([rng.random(3000) * max(total, 1e-300), [total, np.nextafter(total, 0)]])
         assert np.array_equal(gpu.sample_shots(u), cpu.sample_all(u))
+
+
+@pytest.mark.parametrize("dtype", [np.complex128, np.complex64])
+@pytest.mark.parametrize("n", [3, 12, 16])
+def test_sample_all2_counts(qsl, port, dtype, n):
+    """sampleAll2 (measure.cpp:237-267): sorted uniforms merged against an Fp
+    running sum with a strict comparison; uniforms above the total counted
+    nowhere."""
+    rng = np.random.default_rng(60 + n)
+    st = random_state(rng, n, dtype) * (0.9 if n == 12 else 1.0)    # total below 1: some uncounted
+    gpu = qsl.Qubits(state=st, dtype=dtype)
+    cpu = port.PortQubits(n, fp32=dtype == np.complex64, state=st)
+    u = rng.random(6000)
+    if dtype == np.complex64:
+        u = u.astype(np.float32).astype(np.float64)
+    counts = cpu.sample_all2(u)
+    got = gpu.sampleAll2(6000, uniforms=u)
+    assert len(got) == 1 << n
+    assert np.array_equal(np.array([got[i] for i in range(1 << n)], dtype=np.uint64), counts)
+
+
+def test_sample_all2_np(qsl, port):
+    from conftest import random_np_state
+    rng = np.random.default_rng(8)
+    n, w = 12, 5
+    st = random_np_state(rng, n, w)
+    gpu = qsl.QubitsNP(state=st)
+    cpu = port.PortNPQubits(n, w, state=st)
+    u = rng.random(4000)
+    counts = cpu.sample_all2(u)
+    got = gpu.sampleAll2(4000, uniforms=u)
+    keys = port.generate_lookup(n, w)
+    assert sorted(got) == [int(k) for k in keys]
+    assert np.array_equal(np.array([got[int(k)] for k in keys], dtype=np.uint64), counts)

@@ -70,6 +70,7 @@ def test_default_against_reference_fixtures(port, tag):
                 assert sim.prob(t, o) == c["probs"][t, o]
         k, cnt = hist(sim.sample_all(c["u"]))
         assert np.array_equal(k, c["keys"]) and np.array_equal(cnt, c["counts"])
+        assert np.array_equal(sim.sample_all2(c["u2"]), c["counts2"])     # measure.cpp:237-267
         for q, u, out in zip(c["measure_qubits"], c["measure_u"], c["measure_out"]):
             assert sim.measure(int(q), float(u)) == out
         assert np.array_equal(bits(sim.state), bits(c["after_measure"]))
