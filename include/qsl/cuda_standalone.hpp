@@ -7,7 +7,7 @@
  * declarations here have the same layout and names as qsl's:
  *   qsl::complex<Fp>  -- {Fp real; Fp imag;} (include/qsl/utils/complex.hpp:40-49)
  *   qsl::Type         -- the backend enum (include/qsl/qubits.hpp:57-63),
- *                        here with Cuda and CudaNP added
+ *                        here with Cuda, CudaNP and CudaResize added
  *   qsl::Qubits       -- the primary template (include/qsl/qubits.hpp:75)
  */
 #ifndef QSL_CUDA_STANDALONE_HPP
@@ -34,6 +34,7 @@ enum class Type {
     Resize,
     Cuda = 0x100,     ///< GB300 state-vector backend (qsl/qubits/cuda.hpp)
     CudaNP = 0x101,   ///< GB300 number-preserving backend
+    CudaResize = 0x102,   ///< GB300 resizeable backend
 };
 
 template <Type T = Type::Default, std::floating_point Fp = double>

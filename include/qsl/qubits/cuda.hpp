@@ -1,21 +1,23 @@
 /*
  * qsl/qubits/cuda.hpp -- qsl::Qubits on one GB300 GPU.
  *
- *   qsl::Qubits<qsl::Type::Cuda, Fp>    drop-in for Type::Default / Type::Omp
- *   qsl::Qubits<qsl::Type::CudaNP, Fp>  drop-in for Type::NP / Type::OmpNP
+ *   qsl::Qubits<qsl::Type::Cuda, Fp>        drop-in for Type::Default / Type::Omp
+ *   qsl::Qubits<qsl::Type::CudaNP, Fp>      drop-in for Type::NP / Type::OmpNP
+ *   qsl::Qubits<qsl::Type::CudaResize, Fp>  drop-in for Type::Resize
  *
- * Both keep the member signatures of include/qsl/qubits/default.hpp:97-712
- * and np.hpp:100-250 of qsl, so qsl's templated consumers (the Simulator /
+ * They keep the member signatures of include/qsl/qubits/default.hpp:97-712,
+ * np.hpp:100-250 and resize.hpp:46-370 of qsl, so qsl's templated consumers (the Simulator /
  * HasAllGates / HasMeasurement / NPSimulator concepts of concepts.hpp, the
  * Verify checkers, the benchmark Time/Compare templates) instantiate with
  * them unchanged.  Every call goes through the C ABI of include/qslc.h to the
  * CUDA kernels in libqslc.so; the amplitudes live in device memory.
  *
  * Use with qsl's headers: include <qsl/qubits.hpp> first.  qsl's Type enum
- * has no Cuda enumerator; qsl::cuda_type / qsl::cuda_np_type name the two
- * backends (they equal Type::Cuda / Type::CudaNP once those enumerators are
- * added with the values 0x100 / 0x101).  Without qsl's headers, this file
- * pulls in qsl/cuda_standalone.hpp, whose Type enum has both.
+ * has no Cuda enumerator; qsl::cuda_type / qsl::cuda_np_type /
+ * qsl::cuda_resize_type name the three backends (they equal Type::Cuda /
+ * Type::CudaNP / Type::CudaResize once those enumerators are added with the
+ * values 0x100 / 0x101 / 0x102).  Without qsl's headers, this file pulls in
+ * qsl/cuda_standalone.hpp, whose Type enum has all three.
  *
  * Errors: std::logic_error where qsl throws it (size mismatch, mixed
  * Hamming weight, bad number of ones) and for out-of-range qubit indices
@@ -24,8 +26,11 @@
  * Random numbers: each object owns a std::mt19937 with
  * std::uniform_real_distribution<Fp>(0, 1), seeded from std::random_device
  * like qsl::Random (src/utils/random.cpp:33-45); seed() fixes it.  The
- * uniforms are drawn on the host in the reference's order and passed to the
- * device, so a given seed gives the reference's outcomes.
+ * resizeable backend shares one generator per Fp among all its objects, as
+ * qsl's Resize backend does (its `random` is a static member,
+ * resize.hpp:59).  The uniforms are drawn on the host in the reference's
+ * order and passed to the device, so a given seed gives the reference's
+ * outcomes.
  */
 #ifndef QSL_QUBITS_CUDA_HPP
 #define QSL_QUBITS_CUDA_HPP
@@ -54,6 +59,7 @@ namespace qsl {
 
 inline constexpr Type cuda_type = static_cast<Type>(0x100);
 inline constexpr Type cuda_np_type = static_cast<Type>(0x101);
+inline constexpr Type cuda_resize_type = static_cast<Type>(0x102);
 
 namespace cuda_detail {
 
@@ -84,13 +90,26 @@ protected:
     qslc_state *h = nullptr;
     std::mt19937 generator;
     std::uniform_real_distribution<Fp> distribution{Fp(0), Fp(1)};
+    bool shared_rng = false;   // draw from the one generator of all such objects
+
+    struct Shared {
+        std::mt19937 generator{std::random_device{}()};
+        std::uniform_real_distribution<Fp> distribution{Fp(0), Fp(1)};
+    };
+    static Shared &shared()
+    {
+        static Shared s;
+        return s;
+    }
 
     Base() : generator(std::random_device{}()) {}
-    Base(const Base &o) : generator(o.generator), distribution(o.distribution)
+    Base(const Base &o)
+        : generator(o.generator), distribution(o.distribution), shared_rng(o.shared_rng)
     {
         check(qslc_clone(o.h, &h));
     }
-    Base(Base &&o) noexcept : h(o.h), generator(o.generator), distribution(o.distribution)
+    Base(Base &&o) noexcept
+        : h(o.h), generator(o.generator), distribution(o.distribution), shared_rng(o.shared_rng)
     {
         o.h = nullptr;
     }
@@ -99,7 +118,11 @@ protected:
         if (h) qslc_destroy(h);
     }
     void assign(const Base &o) { check(qslc_assign(h, o.h)); }
-    Fp draw() { return distribution(generator); }
+    Fp draw()
+    {
+        if (shared_rng) return shared().distribution(shared().generator);
+        return distribution(generator);
+    }
     void gate1(int g, unsigned t, Fp a = 0) { check(qslc_gate1(h, g, t, double(a))); }
     void gate2(int g, unsigned a, unsigned b, Fp x = 0) { check(qslc_gate2(h, g, a, b, double(x))); }
 
@@ -107,7 +130,16 @@ public:
     using Fp_type = Fp;
 
     /// Fix the generator's seed (qsl::Random has no equivalent).
-    void seed(std::uint32_t s) { generator.seed(s); }
+    void seed(std::uint32_t s)
+    {
+        if (shared_rng) {
+            shared().generator.seed(s);
+            shared().distribution.reset();
+        } else {
+            generator.seed(s);
+            distribution.reset();
+        }
+    }
     /// The C-ABI handle, for callers that mix in qslc_* calls.
     qslc_state *handle() const { return h; }
     /// Wait for every queued kernel of this object.
@@ -238,13 +270,36 @@ public:
     void npHadamard(unsigned q1, unsigned q2) { gate2(QSLC_NP_HADAMARD, q1, q2); }
 };
 
+/* Base plus the gates outside the number-preserving set
+ * (HasNonNPGates, concepts.hpp:84-102). */
+template <std::floating_point Fp>
+class Full : public Base<Fp> {
+public:
+    // One-qubit gates (gates.cpp:32-209)
+    void pauliX(unsigned targ) { this->gate1(QSLC_PAULI_X, targ); }
+    void pauliY(unsigned targ) { this->gate1(QSLC_PAULI_Y, targ); }
+    void hadamard(unsigned targ) { this->gate1(QSLC_HADAMARD, targ); }
+    void rotateX(unsigned targ, Fp angle) { this->gate1(QSLC_ROTATE_X, targ, angle); }
+    void rotateY(unsigned targ, Fp angle) { this->gate1(QSLC_ROTATE_Y, targ, angle); }
+    // Controlled gates (gates.cpp:215-500)
+    void controlNot(unsigned ctrl, unsigned targ) { this->gate2(QSLC_CONTROL_NOT, ctrl, targ); }
+    void controlY(unsigned ctrl, unsigned targ) { this->gate2(QSLC_CONTROL_Y, ctrl, targ); }
+    void controlRotateX(unsigned ctrl, unsigned targ, Fp angle)
+    {
+        this->gate2(QSLC_CONTROL_ROTATE_X, ctrl, targ, angle);
+    }
+    void controlRotateY(unsigned ctrl, unsigned targ, Fp angle)
+    {
+        this->gate2(QSLC_CONTROL_ROTATE_Y, ctrl, targ, angle);
+    }
+    void controlHadamard(unsigned ctrl, unsigned targ) { this->gate2(QSLC_CONTROL_HADAMARD, ctrl, targ); }
+};
+
 }  // namespace cuda_detail
 
 /* Drop-in for Qubits<Type::Default, Fp> (default.hpp:65-713). */
 template <std::floating_point Fp>
-class Qubits<cuda_type, Fp> : public cuda_detail::Base<Fp> {
-    using B = cuda_detail::Base<Fp>;
-
+class Qubits<cuda_type, Fp> : public cuda_detail::Full<Fp> {
 public:
     inline static const std::string name =
         std::is_same_v<Fp, double> ? "Qub<cuda,double>" : "Qub<cuda,float>";
@@ -266,25 +321,60 @@ public:
     Qubits(Qubits &&) noexcept = default;
     /// Copies the amplitudes; throws on a qubit-count mismatch (default.cpp:94-105).
     void operator=(const Qubits &old) { this->assign(old); }
+};
 
-    // One-qubit gates (gates.cpp:32-209)
-    void pauliX(unsigned targ) { this->gate1(QSLC_PAULI_X, targ); }
-    void pauliY(unsigned targ) { this->gate1(QSLC_PAULI_Y, targ); }
-    void hadamard(unsigned targ) { this->gate1(QSLC_HADAMARD, targ); }
-    void rotateX(unsigned targ, Fp angle) { this->gate1(QSLC_ROTATE_X, targ, angle); }
-    void rotateY(unsigned targ, Fp angle) { this->gate1(QSLC_ROTATE_Y, targ, angle); }
-    // Controlled gates (gates.cpp:215-500)
-    void controlNot(unsigned ctrl, unsigned targ) { this->gate2(QSLC_CONTROL_NOT, ctrl, targ); }
-    void controlY(unsigned ctrl, unsigned targ) { this->gate2(QSLC_CONTROL_Y, ctrl, targ); }
-    void controlRotateX(unsigned ctrl, unsigned targ, Fp angle)
+/* Drop-in for Qubits<Type::Resize, Fp> (resize.hpp:46-370): the Default
+ * gates and measurement on a state whose qubit count changes. */
+template <std::floating_point Fp>
+class Qubits<cuda_resize_type, Fp> : public cuda_detail::Full<Fp> {
+public:
+    inline static const std::string name =
+        std::is_same_v<Fp, double> ? "Qub<cuda_resize,double>" : "Qub<cuda_resize,float>";
+    using Fp_type = Fp;
+
+    /// The all-zero state (resize.cpp:39-46).
+    explicit Qubits(unsigned nqubits)
     {
-        this->gate2(QSLC_CONTROL_ROTATE_X, ctrl, targ, angle);
+        this->shared_rng = true;
+        cuda_detail::check(qslc_create_resizable(nqubits, cuda_detail::dtype_of<Fp>, &this->h));
     }
-    void controlRotateY(unsigned ctrl, unsigned targ, Fp angle)
+    /// From a state vector of any power-of-two size (resize.cpp:48-55).
+    explicit Qubits(const std::vector<complex<Fp>> &state)
     {
-        this->gate2(QSLC_CONTROL_ROTATE_Y, ctrl, targ, angle);
+        this->shared_rng = true;
+        unsigned n = cuda_detail::log2_size(state.size());
+        cuda_detail::check(qslc_create_resizable(n, cuda_detail::dtype_of<Fp>, &this->h));
+        this->setState(state);
     }
-    void controlHadamard(unsigned ctrl, unsigned targ) { this->gate2(QSLC_CONTROL_HADAMARD, ctrl, targ); }
+    Qubits(const Qubits &) = default;
+    Qubits(Qubits &&) noexcept = default;
+    /// Takes the other object's qubit count and amplitudes (the implicit
+    /// assignment of resize.hpp; resize.cpp:150-165 is commented out).
+    void operator=(const Qubits &old) { this->assign(old); }
+
+    /// A qubit in |0> at position targ; the qubits at and above it move up
+    /// by one (resize.cpp:106-147).
+    void addQubit(unsigned targ) { cuda_detail::check(qslc_add_qubit(this->h, targ)); }
+    /// addQubit(getNumQubits()) (resize.cpp:100-104).
+    void appendQubit() { addQubit(this->getNumQubits()); }
+    /// Trim the allocation to the live amplitudes (resize.cpp:92-98).
+    void reallocateState() { cuda_detail::check(qslc_reallocate(this->h)); }
+
+    /// measure and remove qubit targ (resize/measure.cpp:156-182)
+    int measureOut(unsigned targ)
+    {
+        const Fp u = this->draw();
+        int out = 0;
+        cuda_detail::check(qslc_measure_out(this->h, targ, double(u), &out));
+        return out;
+    }
+    /// postselect and remove qubit targ (resize/measure.cpp:238-251)
+    Fp postselectOut(unsigned targ, unsigned outcome)
+    {
+        double p = 0;
+        cuda_detail::check(qslc_postselect_out(this->h, targ, outcome, &p));
+        return Fp(p);
+    }
 };
 
 /* Drop-in for Qubits<Type::NP, Fp> (np.hpp:55-253): only the C(n, nones)

@@ -163,6 +163,39 @@ QSLC_API int qslc_measure(qslc_state *s, unsigned targ, double u, int *outcome);
 /* postselect(targ, outcome) (measure.cpp:149-161); returns the probability. */
 QSLC_API int qslc_postselect(qslc_state *s, unsigned targ, unsigned outcome, double *prob);
 
+/* Resizeable states: the qubit-count operations of qsl's Resize backend
+ * (include/qsl/qubits/resize.hpp:46-370).  A resizeable handle keeps a
+ * capacity of allocated amplitudes, 2^n of them live, and accepts in
+ * qslc_set_state any power-of-two size and in qslc_assign another
+ * resizeable state of any size (resize.cpp:67-78).  Gates and measurement
+ * are the Default backend's (resize/gates.cpp, resize/measure.cpp repeat
+ * default/ line for line).  The calls below return QSLC_EINVAL on a handle
+ * not made by qslc_create_resizable. */
+QSLC_API int qslc_create_resizable(unsigned nqubits, int dtype, qslc_state **out);
+QSLC_API int qslc_is_resizable(const qslc_state *s);
+/* allocated amplitudes (the reference's dim_max) */
+QSLC_API uint64_t qslc_capacity(const qslc_state *s);
+
+/* addQubit(targ) (resize.cpp:106-147): a new qubit in |0> at position
+ * targ <= n; the old qubits at and above targ move up by one.  The
+ * capacity doubles when it is full.  appendQubit() is targ = n. */
+QSLC_API int qslc_add_qubit(qslc_state *s, unsigned targ);
+
+/* collapseOut(targ, outcome, factor) (resize/measure.cpp:61-95): keep the
+ * amplitudes with bit targ = outcome, scaled by factor, and remove the
+ * qubit.  EINVAL on a one-qubit state. */
+QSLC_API int qslc_collapse_out(qslc_state *s, unsigned targ, unsigned outcome, double factor);
+
+/* measureOut(targ) (resize/measure.cpp:156-182) with the uniform `u`. */
+QSLC_API int qslc_measure_out(qslc_state *s, unsigned targ, double u, int *outcome);
+
+/* postselectOut(targ, outcome) (resize/measure.cpp:238-251); returns the
+ * probability. */
+QSLC_API int qslc_postselect_out(qslc_state *s, unsigned targ, unsigned outcome, double *prob);
+
+/* reallocateState (resize.cpp:92-98): shrink the capacity to 2^n. */
+QSLC_API int qslc_reallocate(qslc_state *s);
+
 /* sample(targ, nsamples) (measure.cpp:191-216): counts[0], counts[1] for
  * the nshots uniforms u[0..nshots). */
 QSLC_API int qslc_sample(qslc_state *s, unsigned targ, const double *u, uint64_t nshots,

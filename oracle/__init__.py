@@ -99,6 +99,8 @@ def port_lib():
             sig("sample_all", None, vp, C.c_uint, vp, C.c_size_t, vp, vp, vp)
             sig("sample", None, vp, C.c_uint, C.c_uint, vp, C.c_size_t, vp)
             sig("sample_all2", None, vp, C.c_uint, vp, C.c_size_t, vp)
+            sig("add_qubit", None, vp, C.c_uint, C.c_uint)
+            sig("collapse_out", None, vp, C.c_uint, C.c_uint, C.c_uint, fp)
             sig("np_phase1", None, vp, vp, C.c_size_t, C.c_uint, C.c_int, fp, C.c_int)
             sig("np_rz0", None, vp, vp, C.c_size_t, C.c_uint, fp, C.c_int)
             sig("np_gate2", None, vp, vp, C.c_size_t, C.c_int, C.c_uint, C.c_uint, fp, C.c_int)
@@ -219,6 +221,78 @@ class PortQubits:
         counts = np.zeros(1 << self.n, dtype=np.uint64)
         self._f("sample_all2")(_ptr(self.state), self.n, _ptr(u), u.size, _ptr(counts))
         return counts
+
+
+class PortResizeQubits(PortQubits):
+    """Resize backend restatement (src/qubits/resize/*.cpp): the Default
+    arithmetic on a state whose qubit count changes.  ``cap`` mirrors the
+    reference's dim_max: the storage doubles when a qubit is added to a full
+    vector, and is kept when one is removed."""
+
+    def __init__(self, nqubits: int, fp32: bool = False, state=None):
+        super().__init__(nqubits, fp32=fp32, state=state)
+        self.buf = self.state
+        self.cap = self.state.size
+
+    def _live(self):
+        self.state = self.buf[: 1 << self.n]
+
+    def set_state(self, st) -> None:
+        """resize.cpp:67-78: any power-of-two size"""
+        st = np.ascontiguousarray(st, dtype=self.dtype)
+        m = st.size
+        if m < 1 or m & (m - 1):
+            raise ValueError("State vector size is not a power of two")
+        if m > self.cap:
+            self.buf = np.zeros(m, dtype=self.dtype)
+            self.cap = m
+        self.buf[:m] = st
+        self.n = m.bit_length() - 1
+        self._live()
+
+    def add_qubit(self, targ: int) -> None:
+        """resize.cpp:106-147"""
+        dim = 1 << self.n
+        if dim == self.cap:
+            grown = np.zeros(2 * dim, dtype=self.dtype)
+            grown[:dim] = self.buf[:dim]
+            self.buf, self.cap = grown, 2 * dim
+        self._f("add_qubit")(_ptr(self.buf), self.n, targ)
+        self.n += 1
+        self._live()
+
+    def append_qubit(self) -> None:
+        """resize.cpp:100-104"""
+        self.add_qubit(self.n)
+
+    def collapse_out(self, targ: int, outcome: int, factor) -> None:
+        self._f("collapse_out")(_ptr(self.buf), self.n, targ, outcome, self.rdtype(factor))
+        self.n -= 1
+        self._live()
+
+    def measure_out(self, targ: int, u: float) -> int:
+        """resize/measure.cpp:156-182"""
+        p0 = self.rdtype(self.prob(targ, 0))
+        u = self.rdtype(u)
+        one = self.rdtype(1)
+        if u < p0:
+            outcome, factor = 0, one / np.sqrt(p0)
+        else:
+            outcome, factor = 1, one / np.sqrt(one - p0)
+        self.collapse_out(targ, outcome, factor)
+        return outcome
+
+    def postselect_out(self, targ: int, outcome: int) -> float:
+        """resize/measure.cpp:238-251"""
+        p = self.rdtype(self.prob(targ, outcome))
+        self.collapse_out(targ, outcome, self.rdtype(1) / np.sqrt(p))
+        return float(p)
+
+    def reallocate(self) -> None:
+        """resize.cpp:92-98"""
+        self.buf = self.buf[: 1 << self.n].copy()
+        self.cap = self.buf.size
+        self._live()
 
 
 class PortNPQubits:
@@ -342,7 +416,7 @@ class PortNPQubits:
 class RefQubits:
     """The reference's own qsl::Qubits<Type, Fp> (oracle/_ref/libqslref.so)."""
 
-    KINDS = {"Default": 0, "Omp": 1, "NP": 2, "OmpNP": 3}
+    KINDS = {"Default": 0, "Omp": 1, "NP": 2, "OmpNP": 3, "Resize": 4}
 
     def __init__(self, kind: str, nqubits: int = 0, nones: int = 1, fp32: bool = False,
                  nthreads: int = 1, state=None, seed: int | None = None):
@@ -432,6 +506,22 @@ class RefQubits:
         if self.lib.qslref_set_num_ones(self.h, w) != 0:
             raise ValueError("setNumOnes threw")
 
+    # Resize backend (resize.hpp:160-180, :310, :350)
+    def add_qubit(self, t):
+        assert self.lib.qslref_add_qubit(self.h, t) == 0
+
+    def append_qubit(self):
+        assert self.lib.qslref_append_qubit(self.h) == 0
+
+    def measure_out(self, t):
+        return self.lib.qslref_measure_out(self.h, t)
+
+    def postselect_out(self, t, o):
+        return self.lib.qslref_postselect_out(self.h, t, o)
+
+    def reallocate(self):
+        assert self.lib.qslref_reallocate(self.h) == 0
+
 
 def ref_lib():
     global _ref
@@ -468,6 +558,11 @@ def ref_lib():
         sig("qslref_set_basis", C.c_int, vp, C.c_uint64)
         sig("qslref_num_ones", C.c_int, vp)
         sig("qslref_set_num_ones", C.c_int, vp, C.c_uint)
+        sig("qslref_add_qubit", C.c_int, vp, C.c_uint)
+        sig("qslref_append_qubit", C.c_int, vp)
+        sig("qslref_measure_out", C.c_int, vp, C.c_uint)
+        sig("qslref_postselect_out", C.c_double, vp, C.c_uint, C.c_uint)
+        sig("qslref_reallocate", C.c_int, vp)
         sig("qslref_next", C.c_uint64, C.c_uint64)
         sig("qslref_hamming_weight", C.c_uint, C.c_uint64)
         sig("qslref_choose", C.c_uint, C.c_uint, C.c_uint)

@@ -53,6 +53,9 @@ enum {
                              const FP *u, size_t nshots, uint64_t counts[2]); \
     void port_##SFX##_sample_all2(const FP *s, unsigned n, const FP *u_sorted,\
                                   size_t nshots, uint64_t *counts);           \
+    void port_##SFX##_add_qubit(FP *s, unsigned n, unsigned targ);            \
+    void port_##SFX##_collapse_out(FP *s, unsigned n, unsigned targ,          \
+                                   unsigned o, FP factor);                    \
     void port_##SFX##_np_phase1(FP *s, const uint64_t *tab, size_t len,       \
                                 unsigned targ, int mode, FP a, int nth);      \
     void port_##SFX##_np_rz0(FP *s, const uint64_t *tab, size_t len,          \

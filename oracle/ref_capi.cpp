@@ -22,7 +22,7 @@
 
 namespace {
 
-enum Kind { K_DEFAULT = 0, K_OMP = 1, K_NP = 2, K_OMPNP = 3 };
+enum Kind { K_DEFAULT = 0, K_OMP = 1, K_NP = 2, K_OMPNP = 3, K_RESIZE = 4 };
 
 struct Base {
     virtual ~Base() = default;
@@ -44,6 +44,12 @@ struct Base {
     virtual int num_ones() const = 0;
     virtual int set_num_ones(unsigned w) = 0;
     virtual unsigned num_qubits() const = 0;
+    // Resize backend only (resize.hpp:160-180, :310, :350); -2 elsewhere
+    virtual int add_qubit(unsigned t) = 0;
+    virtual int append_qubit() = 0;
+    virtual int measure_out(unsigned t) = 0;
+    virtual double postselect_out(unsigned t, unsigned o) = 0;
+    virtual int reallocate() = 0;
 };
 
 template <class S>
@@ -136,6 +142,31 @@ struct Impl final : Base {
         return -2;
     }
     unsigned num_qubits() const override { return sim.getNumQubits(); }
+    int add_qubit(unsigned t) override
+    {
+        if constexpr (requires(S &s) { s.addQubit(0u); }) { sim.addQubit(t); return 0; }
+        return -2;
+    }
+    int append_qubit() override
+    {
+        if constexpr (requires(S &s) { s.appendQubit(); }) { sim.appendQubit(); return 0; }
+        return -2;
+    }
+    int measure_out(unsigned t) override
+    {
+        if constexpr (requires(S &s) { s.measureOut(0u); }) return sim.measureOut(t);
+        return -2;
+    }
+    double postselect_out(unsigned t, unsigned o) override
+    {
+        if constexpr (requires(S &s) { s.postselectOut(0u, 0u); }) return sim.postselectOut(t, o);
+        return -2;
+    }
+    int reallocate() override
+    {
+        if constexpr (requires(S &s) { s.reallocateState(); }) { sim.reallocateState(); return 0; }
+        return -2;
+    }
 };
 
 template <class Fp>
@@ -154,6 +185,7 @@ Base *make(int kind, unsigned n, unsigned nones, unsigned nth)
     case K_OMP: return new Impl<qsl::Qubits<qsl::Type::Omp, Fp>>(n, nth);
     case K_NP: return new Impl<qsl::Qubits<qsl::Type::NP, Fp>>(n, nones);
     case K_OMPNP: return new Impl<qsl::Qubits<qsl::Type::OmpNP, Fp>>(n, nones, nth);
+    case K_RESIZE: return new Impl<qsl::Qubits<qsl::Type::Resize, Fp>>(n);
     }
     return nullptr;
 }
@@ -167,6 +199,7 @@ Base *make_from(int kind, const void *in, std::size_t d, unsigned nth)
     case K_OMP: return new Impl<qsl::Qubits<qsl::Type::Omp, Fp>>(v, nth);
     case K_NP: return new Impl<qsl::Qubits<qsl::Type::NP, Fp>>(v);
     case K_OMPNP: return new Impl<qsl::Qubits<qsl::Type::OmpNP, Fp>>(v, nth);
+    case K_RESIZE: return new Impl<qsl::Qubits<qsl::Type::Resize, Fp>>(v);
     }
     return nullptr;
 }
@@ -250,6 +283,14 @@ void qslref_reset(void *h) { static_cast<Base *>(h)->reset(); }
 int qslref_set_basis(void *h, std::uint64_t idx) { return static_cast<Base *>(h)->set_basis(idx); }
 int qslref_num_ones(void *h) { return static_cast<Base *>(h)->num_ones(); }
 int qslref_set_num_ones(void *h, unsigned w) { return static_cast<Base *>(h)->set_num_ones(w); }
+int qslref_add_qubit(void *h, unsigned t) { return static_cast<Base *>(h)->add_qubit(t); }
+int qslref_append_qubit(void *h) { return static_cast<Base *>(h)->append_qubit(); }
+int qslref_measure_out(void *h, unsigned t) { return static_cast<Base *>(h)->measure_out(t); }
+double qslref_postselect_out(void *h, unsigned t, unsigned o)
+{
+    return static_cast<Base *>(h)->postselect_out(t, o);
+}
+int qslref_reallocate(void *h) { return static_cast<Base *>(h)->reallocate(); }
 
 // src/utils/misc.cpp
 std::uint64_t qslref_next(std::uint64_t x)

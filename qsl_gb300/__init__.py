@@ -74,6 +74,14 @@ SIGNATURES = {
     "qslc_flush": (C.c_int, [_VP]),
     "qslc_set_fusion_tc": (C.c_int, [_VP, C.c_int]),
     "qslc_fused_blocks": (C.c_uint64, [_VP]),
+    "qslc_create_resizable": (C.c_int, [C.c_uint, C.c_int, C.POINTER(C.c_void_p)]),
+    "qslc_is_resizable": (C.c_int, [_VP]),
+    "qslc_capacity": (C.c_uint64, [_VP]),
+    "qslc_add_qubit": (C.c_int, [_VP, C.c_uint]),
+    "qslc_collapse_out": (C.c_int, [_VP, C.c_uint, C.c_uint, C.c_double]),
+    "qslc_measure_out": (C.c_int, [_VP, C.c_uint, C.c_double, C.POINTER(C.c_int)]),
+    "qslc_postselect_out": (C.c_int, [_VP, C.c_uint, C.c_uint, C.POINTER(C.c_double)]),
+    "qslc_reallocate": (C.c_int, [_VP]),
     "qslc_batch_create": (C.c_int, [C.c_int, C.c_uint32, _VP, _VP, C.c_uint32,
                                     C.POINTER(C.c_void_p)]),
     "qslc_batch_run": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
@@ -327,6 +335,50 @@ def _mk(name):
 
 for _g in list(GATE1) + list(GATE2):
     setattr(Qubits, _g, _mk(_g))
+
+
+class QubitsResize(Qubits):
+    """qsl::Qubits<Type::Resize>: the Default arithmetic on a state whose
+    qubit count changes (include/qsl/qubits/resize.hpp:46-370).
+    ``setState`` takes any power-of-two size, ``assign`` any resizeable
+    state."""
+
+    def __init__(self, nqubits=None, dtype=np.complex128, state=None, seed=None, _handle=None):
+        if state is not None and nqubits is None:
+            st = np.ascontiguousarray(state, dtype=dtype)
+            nqubits = max(st.size.bit_length() - 1, 1)
+        super().__init__(nqubits, dtype=dtype, state=state, seed=seed, _handle=_handle)
+
+    def _create(self, n, h):
+        return self.L.qslc_create_resizable(n, self.code, C.byref(h))
+
+    def capacity(self) -> int:
+        """allocated amplitudes (the reference's dim_max)"""
+        return int(self.L.qslc_capacity(self.h))
+
+    def addQubit(self, targ: int) -> None:
+        _check(self.L.qslc_add_qubit(self.h, targ))
+
+    def appendQubit(self) -> None:
+        self.addQubit(self.nqubits)
+
+    def reallocateState(self) -> None:
+        _check(self.L.qslc_reallocate(self.h))
+
+    def collapseOut(self, targ: int, outcome: int, factor: float) -> None:
+        _check(self.L.qslc_collapse_out(self.h, targ, outcome, float(factor)))
+
+    def measureOut(self, targ: int, u: float | None = None) -> int:
+        if u is None:
+            u = self.rng.random()
+        out = C.c_int()
+        _check(self.L.qslc_measure_out(self.h, targ, float(u), C.byref(out)))
+        return out.value
+
+    def postselectOut(self, targ: int, outcome: int) -> float:
+        out = C.c_double()
+        _check(self.L.qslc_postselect_out(self.h, targ, outcome, C.byref(out)))
+        return out.value
 
 
 class QubitsNP(Qubits):

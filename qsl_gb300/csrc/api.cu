@@ -94,10 +94,14 @@ int flushed(qslc_state *s)
 int alloc_amps(qslc_state *s, uint64_t count)
 {
     if (count == 0) return fail(QSLC_EINVAL, "no amplitudes to allocate");
-    if (s->amps && s->namps == count) return QSLC_OK;
+    if (s->amps && s->cap == count) {
+        s->namps = count;
+        return QSLC_OK;
+    }
     if (s->amps) cudaFree(s->amps);
     s->amps = nullptr;
     s->namps = 0;
+    s->cap = 0;
     void *p = nullptr;
     cudaError_t e = cudaMalloc(&p, count * s->amp_bytes());
     if (e != cudaSuccess) {
@@ -107,6 +111,7 @@ int alloc_amps(qslc_state *s, uint64_t count)
     }
     s->amps = p;
     s->namps = count;
+    s->cap = count;
     return QSLC_OK;
 }
 
@@ -269,6 +274,7 @@ int qslc_clone(const qslc_state *src, qslc_state **out)
     if (rc) return rc;
     qslc_state *s = *out;
     s->np = src->np;
+    s->resizable = src->resizable;
     if (src->np) rc = np_set_weight(s, src->nones);
     else rc = alloc_amps(s, src->namps);
     if (!rc) s->fuse_k = src->fuse_k;
@@ -290,14 +296,22 @@ int qslc_assign(qslc_state *dst, const qslc_state *src)
     int rc = check_handle(dst);
     if (!rc) rc = check_handle(src);
     if (rc) return rc;
-    if (dst->n != src->n)
-        return fail(QSLC_ESIZE, "Cannot assign Qubits object vector from different number of qubits");
-    if (dst->dtype != src->dtype || dst->np != src->np)
+    if (dst->dtype != src->dtype || dst->np != src->np || dst->resizable != src->resizable)
         return fail(QSLC_EINVAL, "cannot assign between different simulator types");
+    // a resizeable state takes the other's qubit count (resize.hpp: the
+    // implicit assignment copies nqubits and dim)
+    if (dst->n != src->n && !dst->resizable)
+        return fail(QSLC_ESIZE, "Cannot assign Qubits object vector from different number of qubits");
     if (dst == src) return flushed(dst);
     rc = flushed(const_cast<qslc_state *>(src));
     if (rc) return rc;
     dst->fuse_queue.clear();                 // overwritten below
+    if (dst->resizable && dst->namps != src->namps) {
+        rc = resize_capacity(dst, src->namps);
+        if (rc) return rc;
+        dst->n = src->n;
+        dst->namps = src->namps;
+    }
     if (dst->np && dst->nones != src->nones) {
         rc = np_set_weight(dst, src->nones);
         if (rc) return rc;
@@ -344,10 +358,19 @@ int qslc_set_state(qslc_state *s, const void *amps, uint64_t n_amps)
 {
     int rc = check_handle(s);
     if (rc) return rc;
-    const uint64_t dim = uint64_t(1) << s->n;
+    uint64_t dim = uint64_t(1) << s->n;
+    if (!amps) return fail(QSLC_EINVAL, "null amplitude pointer");
+    if (n_amps != dim && s->resizable) {
+        // any power of two (resize.cpp:67-78, quantum.cpp:109-130)
+        if (n_amps < 2 || (n_amps & (n_amps - 1)) || n_amps > (uint64_t(1) << MAX_QUBITS))
+            return fail(QSLC_ESIZE, "State vector size is not a power of two");
+        rc = resize_capacity(s, n_amps);
+        if (rc) return rc;
+        s->n = unsigned(__builtin_ctzll(n_amps));
+        s->namps = dim = n_amps;
+    }
     if (n_amps != dim)
         return fail(QSLC_ESIZE, "Cannot assign state vector from different number of qubits");
-    if (!amps) return fail(QSLC_EINVAL, "null amplitude pointer");
     s->fuse_queue.clear();
     if (!s->np) {
         QSLC_CUDA(cudaMemcpyAsync(s->amps, amps, dim * s->amp_bytes(), cudaMemcpyHostToDevice, s->stream));
@@ -489,6 +512,95 @@ int qslc_postselect(qslc_state *s, unsigned targ, unsigned outcome, double *prob
     if (rc) return rc;
     if (prob) *prob = p;
     return QSLC_OK;
+}
+
+// ---- resizeable states (qsl's Resize backend) ------------------------------
+
+int qslc_create_resizable(unsigned nqubits, int dtype, qslc_state **out)
+{
+    int rc = qslc_create(nqubits, dtype, out);
+    if (!rc) (*out)->resizable = 1;
+    return rc;
+}
+
+int qslc_is_resizable(const qslc_state *s) { return s ? s->resizable : 0; }
+uint64_t qslc_capacity(const qslc_state *s) { return s ? s->cap : 0; }
+
+static int check_resizable(const qslc_state *s)
+{
+    int rc = check_handle(s);
+    if (rc) return rc;
+    if (!s->resizable) return fail(QSLC_EINVAL, "not a resizeable state");
+    return QSLC_OK;
+}
+
+int qslc_add_qubit(qslc_state *s, unsigned targ)
+{
+    int rc = check_resizable(s);
+    if (rc) return rc;
+    if (targ > s->n)
+        return fail(QSLC_EINVAL, "new qubit position " + std::to_string(targ) + " above the " +
+                                     std::to_string(s->n) + " existing qubits");
+    if (s->n + 1 > MAX_QUBITS)
+        return fail(QSLC_EINVAL, "at most " + std::to_string(MAX_QUBITS) + " qubits");
+    rc = flushed(s);
+    if (rc) return rc;
+    return resize_add_qubit(s, targ);
+}
+
+int qslc_collapse_out(qslc_state *s, unsigned targ, unsigned outcome, double factor)
+{
+    int rc = check_resizable(s);
+    if (!rc) rc = check_q(s, targ);
+    if (rc) return rc;
+    if (outcome > 1) return fail(QSLC_EINVAL, "outcome must be 0 or 1");
+    if (s->n < 2) return fail(QSLC_EINVAL, "cannot remove the last qubit");
+    rc = flushed(s);
+    if (rc) return rc;
+    return resize_collapse_out(s, targ, outcome, factor, s->fuse_k && s->dtype == QSLC_C64);
+}
+
+int qslc_measure_out(qslc_state *s, unsigned targ, double u, int *outcome)
+{
+    int rc = check_resizable(s);
+    if (rc) return rc;
+    if (s->n < 2) return fail(QSLC_EINVAL, "cannot remove the last qubit");
+    double p0;
+    rc = qslc_prob(s, targ, 0, &p0);
+    if (rc) return rc;
+    int o;
+    double factor;
+    if (s->dtype == QSLC_C128 || s->fuse_k) decide<double>(p0, u, &o, &factor);
+    else decide<float>(p0, u, &o, &factor);
+    rc = qslc_collapse_out(s, targ, unsigned(o), factor);
+    if (rc) return rc;
+    if (outcome) *outcome = o;
+    return QSLC_OK;
+}
+
+int qslc_postselect_out(qslc_state *s, unsigned targ, unsigned outcome, double *prob)
+{
+    int rc = check_resizable(s);
+    if (rc) return rc;
+    if (s->n < 2) return fail(QSLC_EINVAL, "cannot remove the last qubit");
+    double p;
+    rc = qslc_prob(s, targ, outcome, &p);
+    if (rc) return rc;
+    double factor;
+    if (s->dtype == QSLC_C128 || s->fuse_k) factor = 1 / std::sqrt(p);   // resize/measure.cpp:243-244
+    else factor = double(1.0f / std::sqrt(float(p)));
+    rc = qslc_collapse_out(s, targ, outcome, factor);
+    if (rc) return rc;
+    if (prob) *prob = p;
+    return QSLC_OK;
+}
+
+int qslc_reallocate(qslc_state *s)
+{
+    int rc = check_resizable(s);
+    if (!rc) rc = flushed(s);
+    if (rc) return rc;
+    return resize_reallocate(s);
 }
 
 int qslc_sample(qslc_state *s, unsigned targ, const double *u, uint64_t nshots, uint64_t counts[2])

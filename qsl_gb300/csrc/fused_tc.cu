@@ -63,13 +63,12 @@ __device__ __forceinline__ uint32_t to_tf32(float x)
     return r;
 }
 
-__device__ __forceinline__ void split_store(unsigned char *hi, unsigned char *lo, uint32_t off, float x)
+// TF32 split of four consecutive K entries of one row: x = hi + lo.
+__device__ __forceinline__ void split4(float4 x, uint4 &hi, uint4 &lo)
 {
-    const uint32_t h = to_tf32(x);
-    const float rest = x - __uint_as_float(h);
-    const uint32_t l = to_tf32(rest);
-    *reinterpret_cast<uint32_t *>(hi + off) = h;
-    *reinterpret_cast<uint32_t *>(lo + off) = l;
+    hi = make_uint4(to_tf32(x.x), to_tf32(x.y), to_tf32(x.z), to_tf32(x.w));
+    lo = make_uint4(to_tf32(x.x - __uint_as_float(hi.x)), to_tf32(x.y - __uint_as_float(hi.y)),
+                    to_tf32(x.z - __uint_as_float(hi.z)), to_tf32(x.w - __uint_as_float(hi.w)));
 }
 
 __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t acc)
@@ -105,6 +104,13 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16])
 }
 
 // bmat: B_hi then B_lo, each [64 n][64 k] row-major fp32 (tf32 values).
+//
+// Pipeline per tile: the 32 amplitudes of this thread's group wait in
+// registers; they are split into shared memory (16-byte stores, one row of
+// a core matrix each), one thread issues the MMAs, and while they run every
+// thread already loads the next tile's amplitudes into the same registers.
+// Tiles cover disjoint groups, so reading the next tile before the current
+// one is written back is safe.
 __global__ void __launch_bounds__(TC_M) k_dense_tc(float2 *__restrict__ st, uint64_t ngroups,
                                                    const float *__restrict__ bmat, uint4 pos_lo,
                                                    unsigned pos_hi, int *__restrict__ err)
@@ -115,16 +121,15 @@ __global__ void __launch_bounds__(TC_M) k_dense_tc(float2 *__restrict__ st, uint
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_slot;
     __shared__ int arrived;
+    __shared__ uint64_t s_off[32];
     const int tid = threadIdx.x, warp = tid >> 5;
     const unsigned pos[5] = {pos_lo.x, pos_lo.y, pos_lo.z, pos_lo.w, pos_hi};
-    uint64_t off[32];
-#pragma unroll
-    for (int v = 0; v < 32; v++) {
+    if (tid < 32) {
         uint64_t o = 0;
 #pragma unroll
         for (int j = 0; j < 5; j++)
-            if (v & (1 << j)) o |= uint64_t(1) << pos[j];
-        off[v] = o;
+            if (tid & (1 << j)) o |= uint64_t(1) << pos[j];
+        s_off[tid] = o;
     }
     // B into the canonical layout (rows n, columns k)
     for (int i = tid; i < TC_N * TC_K; i += TC_M) {
@@ -153,18 +158,31 @@ __global__ void __launch_bounds__(TC_M) k_dense_tc(float2 *__restrict__ st, uint
     const uint32_t b_hi_s = uint32_t(__cvta_generic_to_shared(b_hi));
     const uint32_t b_lo_s = uint32_t(__cvta_generic_to_shared(b_lo));
     const uint64_t ntiles = ngroups / TC_M;
+    auto group_base = [&](uint64_t t) {
+        uint64_t b = t * TC_M + tid;
+#pragma unroll
+        for (int j = 0; j < 5; j++) b = insert0(b, pos[j]);
+        return b;
+    };
+    float2 a[32];
+    uint64_t t = blockIdx.x;
+    if (t < ntiles) {
+        const uint64_t b0 = group_base(t);
+#pragma unroll
+        for (int v = 0; v < 32; v++) a[v] = st[b0 | s_off[v]];
+    }
     uint32_t phase = 0;
     bool ok = true;
-    for (uint64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-        // this thread's group: row `tid` of the tile
-        uint64_t base = t * TC_M + tid;
+    for (; t < ntiles && ok; t += gridDim.x) {
+        const uint64_t base = group_base(t);
+        // row `tid` of A: K entries 4j..4j+3 are amplitudes 2j, 2j+1 as (re, im)
 #pragma unroll
-        for (int j = 0; j < 5; j++) base = insert0(base, pos[j]);
-#pragma unroll 8
-        for (int v = 0; v < 32; v++) {
-            const float2 a = st[base | off[v]];
-            split_store(a_hi, a_lo, core_offset(tid, 2 * v), a.x);
-            split_store(a_hi, a_lo, core_offset(tid, 2 * v + 1), a.y);
+        for (int j = 0; j < 16; j++) {
+            uint4 hi, lo;
+            split4(make_float4(a[2 * j].x, a[2 * j].y, a[2 * j + 1].x, a[2 * j + 1].y), hi, lo);
+            const uint32_t o = core_offset(tid, 4 * j);
+            *reinterpret_cast<uint4 *>(a_hi + o) = hi;
+            *reinterpret_cast<uint4 *>(a_lo + o) = lo;
         }
         asm volatile("fence.proxy.async.shared::cta;");
         asm volatile("tcgen05.fence::before_thread_sync;");
@@ -182,6 +200,13 @@ __global__ void __launch_bounds__(TC_M) k_dense_tc(float2 *__restrict__ st, uint
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                 mbar_s));
+        }
+        // the next tile's amplitudes travel while the MMAs run
+        const uint64_t tn = t + gridDim.x;
+        if (tn < ntiles) {
+            const uint64_t bn = group_base(tn);
+#pragma unroll
+            for (int v = 0; v < 32; v++) a[v] = st[bn | s_off[v]];
         }
         // one thread polls the barrier (bounded); the block follows its verdict
         if (tid == 0) arrived = mbar_wait(mbar_s, phase) ? 1 : 0;
@@ -206,7 +231,7 @@ __global__ void __launch_bounds__(TC_M) k_dense_tc(float2 *__restrict__ st, uint
 #pragma unroll
             for (int i = 0; i < 8; i++) {
                 const int v = 8 * c + i;
-                st[base | off[v]] = make_float2(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]));
+                st[base | s_off[v]] = make_float2(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]));
             }
         }
         asm volatile("tcgen05.fence::before_thread_sync;");

@@ -98,7 +98,9 @@ struct qslc_state {
     int dtype = QSLC_C128;    // QSLC_C128 or QSLC_C64
     int np = 0;               // 1: number-preserving (compressed) layout
     unsigned nones = 0;       // Hamming weight of an NP state
-    uint64_t namps = 0;       // amplitudes held on the device
+    uint64_t namps = 0;       // live amplitudes (2^n, or C(n, w) for NP)
+    uint64_t cap = 0;         // amplitudes allocated (>= namps)
+    int resizable = 0;        // 1: qubits may be added and removed (resize.cu)
     void *amps = nullptr;     // device amplitudes
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -146,6 +148,12 @@ int launch_fill_basis(qslc_state *s, uint64_t pos);
 
 // fused.cu
 int fusion_flush(qslc_state *s);
+
+// resize.cu
+int resize_add_qubit(qslc_state *s, unsigned targ);
+int resize_collapse_out(qslc_state *s, unsigned targ, unsigned outcome, double factor, bool f64);
+int resize_reallocate(qslc_state *s);
+int resize_capacity(qslc_state *s, uint64_t count);   // grow the allocation; contents undefined
 
 // fused_tc.cu
 void tc_pack_block(const std::vector<cd> &U, float *out);

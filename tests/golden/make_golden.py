@@ -150,6 +150,95 @@ def case_layered(seed, n, layers, nshots):
                 **dict(zip(("names", "q1", "q2", "ang"), encode(circ))))
 
 
+RESIZE_OPS = ("gate", "add_qubit", "append_qubit", "measure_out", "postselect_out",
+              "reallocate", "set_state")
+
+
+def random_state(rng, n, dt):
+    v = rng.uniform(-1, 1, 1 << n) + 1j * rng.uniform(-1, 1, 1 << n)
+    return (v / np.linalg.norm(v)).astype(dt)
+
+
+def case_resize(seed, n0, steps, fp32):
+    """The Resize backend through a random script of gates, addQubit,
+    appendQubit, measureOut, postselectOut, reallocateState and setState
+    with a new size; the state (and the outcome or probability) after
+    every step, then every prob and sampleAll.  Step i is RESIZE_OPS[kind[i]]
+    with arguments qa[i], qb[i], x[i] (gate: ALL_NAMES[gate[i]] on qa, qb,
+    angle x; measure_out: qubit qa, uniform x; postselect_out: qubit qa,
+    outcome qb; set_state: a new state of qa qubits, stored in states)."""
+    rng = np.random.default_rng(seed)
+    dt = np.complex64 if fp32 else np.complex128
+    init = random_state(rng, n0, dt)
+    ref = oracle.RefQubits("Resize", fp32=fp32, state=init)
+    kind, gate, qa, qb, xs, res, states = [], [], [], [], [], [], []
+    # The reference's storage: dim_max and the vector's size.  Its
+    # reallocateState and setState leave dim_max as it was (resize.cpp:67-98),
+    # after which addQubit can write past the vector's end
+    # (resize.cpp:111-140); the script adds a qubit only where the
+    # reference stays inside its vector.
+    dim_max = size = 1 << n0
+    for _ in range(steps):
+        n = ref.n
+        dim = 1 << n
+        r = rng.random()
+        g, a, b, x, out = -1, 0, -1, 0.0, 0.0
+        if 0.4 <= r < 0.68 and not (dim == dim_max or 2 * dim <= size):
+            continue
+        if r < 0.4:
+            k = 0
+            g = int(rng.integers(len(ALL_NAMES)))
+            a, b = (int(v) for v in rng.choice(n, 2, replace=False))
+            if ALL_NAMES[g] in GATES1:
+                b = -1
+            x = float(rng.uniform(0, 2 * np.pi))
+            if fp32:
+                x = float(np.float32(x))
+            workloads.apply(ref, [(ALL_NAMES[g], a, None if b < 0 else b, x)])
+        elif r < 0.68 and n < 10:
+            if dim == dim_max:
+                size = dim_max = 2 * dim
+            if r < 0.62:
+                k, a = 1, int(rng.integers(n + 1))
+                ref.add_qubit(a)
+            else:
+                k = 2
+                ref.append_qubit()
+        elif r < 0.8 and n > 2:
+            k, a = 3, int(rng.integers(n))
+            x = float(uniforms(rng, 1, fp32)[0])
+            oracle.ref_feed_uniforms([x])
+            out = float(ref.measure_out(a))
+        elif r < 0.92 and n > 2:
+            k, a, b = 4, int(rng.integers(n)), int(rng.integers(2))
+            if ref.prob(a, b) < 1e-3:
+                b ^= 1
+            out = float(ref.postselect_out(a, b))
+        elif r < 0.96:
+            k = 5
+            ref.reallocate()
+            size = dim
+        else:
+            k, a = 6, int(rng.integers(2, 10))
+            ref.set_state(random_state(rng, a, dt))
+            size = 1 << a
+        kind.append(k)
+        gate.append(g)
+        qa.append(a)
+        qb.append(b)
+        xs.append(x)
+        res.append(out)
+        states.append(ref.get_state())
+    n = ref.n
+    probs = np.array([[ref.prob(t, o) for o in (0, 1)] for t in range(n)])
+    u = uniforms(rng, 500, fp32)
+    keys, counts = feed_map(ref, u)
+    return dict(init=init, kind=np.array(kind, dtype=np.int32), gate=np.array(gate, dtype=np.int32),
+                qa=np.array(qa, dtype=np.int32), qb=np.array(qb, dtype=np.int32), x=np.array(xs),
+                res=np.array(res), state_len=np.array([st.size for st in states], dtype=np.int64),
+                states=np.concatenate(states), probs=probs, u=u, keys=keys, counts=counts)
+
+
 def kats():
     lib = oracle.ref_lib()
     seq = [0b111]
@@ -178,6 +267,11 @@ def main():
         cases = {"n8w4": case_np(11, 8, 4, fp32), "n10w3": case_np(12, 10, 3, fp32),
                  "n6w1": case_np(13, 6, 1, fp32)}
         np.savez_compressed(os.path.join(HERE, f"np_{tag}.npz"),
+                            **{f"{k}__{f}": v for k, c in cases.items() for f, v in c.items()})
+    for fp32 in (False, True):
+        tag = "c64" if fp32 else "c128"
+        cases = {f"r{s}": case_resize(s, 5, 60, fp32) for s in (31, 32, 33)}
+        np.savez_compressed(os.path.join(HERE, f"resize_{tag}.npz"),
                             **{f"{k}__{f}": v for k, c in cases.items() for f, v in c.items()})
     lay = case_layered(2021, 12, 20, 10000)
     np.savez_compressed(os.path.join(HERE, "layered_n12.npz"), **lay)

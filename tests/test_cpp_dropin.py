@@ -32,6 +32,21 @@ def test_concepts_with_qsl_headers():
         os.path.join(CPP, "concepts_check.cpp"))
 
 
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF_INC, "qsl")), reason="qsl headers absent")
+def test_verify_checkers_instantiate_and_link(qsl, tmp_path):
+    """qsl::Verify with every checker of qsl's framework, CUDA backends as the
+    second simulator, compiled against qsl's headers and linked against qsl's
+    Default/NP implementation (oracle/_ref) and libqslc.  Running it needs
+    those headers and a GPU on one machine."""
+    import oracle
+    oracle.build(reference=True)
+    libdir = os.path.dirname(qsl.LIB_PATH)
+    refdir = os.path.dirname(oracle.REF_SO)
+    gxx("-O1", "-fopenmp", "-I", os.path.join(ROOT, "include"), "-I", REF_INC,
+        os.path.join(CPP, "verify_check.cpp"), "-o", str(tmp_path / "verify_check"),
+        "-L", libdir, "-lqslc", "-L", refdir, "-lqslref", f"-Wl,-rpath,{libdir}:{refdir}")
+
+
 def build_drop_in(qsl, tmp):
     exe = os.path.join(tmp, "drop_in")
     libdir = os.path.dirname(qsl.LIB_PATH)

@@ -110,6 +110,22 @@ def test_layered_against_reference_fixture(port):
     assert sim.measure_all(float(c["measure_all_u"][0])) == int(c["measure_all"])
 
 
+@pytest.mark.parametrize("tag", ["c128", "c64"])
+def test_resize_against_reference_fixtures(port, tag):
+    """The Resize backend's script (addQubit, appendQubit, measureOut,
+    postselectOut, reallocateState, setState of a new size, gates) replayed
+    on the restatement, step by step against the reference's states."""
+    from resize_replay import replay
+    dtype = np.complex64 if tag == "c64" else np.complex128
+    for name, c in load(f"resize_{tag}.npz").items():
+        sim = port.PortResizeQubits(int(np.log2(c["init"].size)), fp32=tag == "c64", state=c["init"])
+        ops = dict(gate=sim.gate, add_qubit=sim.add_qubit, append_qubit=sim.append_qubit,
+                   measure_out=sim.measure_out, postselect_out=sim.postselect_out,
+                   reallocate=sim.reallocate, set_state=sim.set_state,
+                   get_state=lambda: sim.state.copy(), prob=sim.prob, sample_all=sim.sample_all)
+        replay(c, ops, dtype, exact=tag == "c128")
+
+
 ref_needed = pytest.mark.skipif(
     not os.path.isdir(os.path.join(os.environ.get("QSL_REFERENCE_SRC", "/root/reference"), "src")),
     reason="reference source tree absent; the committed fixtures pin the oracle")
