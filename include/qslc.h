@@ -237,8 +237,9 @@ QSLC_API uint64_t qslc_launch_count(const qslc_state *s);
  * for bit.  0 turns fusion off (after applying what is queued). */
 QSLC_API int qslc_set_fusion(qslc_state *s, unsigned max_qubits);
 QSLC_API int qslc_flush(qslc_state *s);
-/* Apply five-qubit blocks on the tensor cores (tcgen05, 3xTF32 split with
- * FP32 accumulation) instead of the CUDA cores; states of 12 qubits or more. */
+/* Five-qubit blocks on states of 12 qubits or more run on the tensor cores
+ * (tcgen05, 3xTF32 split with FP32 accumulation); this is the default.
+ * on = 0 applies them on the CUDA cores instead. */
 QSLC_API int qslc_set_fusion_tc(qslc_state *s, int on);
 /* Fused blocks applied through this handle so far. */
 QSLC_API uint64_t qslc_fused_blocks(const qslc_state *s);

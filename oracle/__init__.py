@@ -570,6 +570,8 @@ def ref_lib():
         sig("qslref_check_state_np", C.c_int, vp, C.c_size_t)
         sig("qslref_check_state_size", C.c_int, C.c_size_t)
         sig("qslref_fubini_study", C.c_double, vp, vp, C.c_size_t)
+        sig("qslref_results_write", C.c_int, C.c_char_p, C.c_char_p, C.c_char_p, C.c_size_t,
+            C.c_size_t, vp, C.c_size_t, vp)
         _ref = lib
     return _ref
 

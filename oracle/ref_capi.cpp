@@ -16,6 +16,8 @@
 #include <string>
 #include <vector>
 
+#include <cmath>   // results.tpp uses std::pow without including it
+#include "qsl/benchmark/results.hpp"
 #include "qsl/qubits.hpp"
 #include "qsl/utils/misc.hpp"
 #include "qsl/utils/quantum.hpp"
@@ -307,6 +309,36 @@ std::size_t qslref_generate_lookup(unsigned len, unsigned ones, std::uint64_t *o
     auto v = qsl::generateLookup(len, ones);
     for (std::size_t i = 0; i < v.size() && i < cap; i++) out[i] = v[i];
     return v.size();
+}
+
+// include/qsl/benchmark/results.tpp: a Results<unsigned, double> of nrows
+// rows (nint integer then nfp floating-point columns, row-major), headings
+// and metadata as '\n'-separated lists, written by writeToFile.
+int qslref_results_write(const char *path, const char *headings, const char *meta,
+                         std::size_t nrows, std::size_t nint, const unsigned *ints, std::size_t nfp,
+                         const double *fps)
+{
+    auto split = [](const char *s) {
+        std::vector<std::string> out;
+        std::string cur;
+        for (; *s; s++) {
+            if (*s == '\n') { out.push_back(cur); cur.clear(); }
+            else cur += *s;
+        }
+        if (!cur.empty()) out.push_back(cur);
+        return out;
+    };
+    try {
+        qsl::Results<unsigned, double> r{split(headings)};
+        for (const auto &m : split(meta)) r.addMeta(m);
+        for (std::size_t i = 0; i < nrows; i++)
+            r.addRow(std::vector<unsigned>(ints + i * nint, ints + (i + 1) * nint),
+                     std::vector<double>(fps + i * nfp, fps + (i + 1) * nfp));
+        r.writeToFile(path);
+    } catch (const std::logic_error &) {
+        return -1;
+    }
+    return 0;
 }
 
 // src/utils/quantum.cpp

@@ -240,7 +240,8 @@ class Qubits:
         _check(self.L.qslc_flush(self.h))
 
     def set_fusion_tc(self, on: bool) -> None:
-        """Apply five-qubit fused blocks on the tensor cores (tcgen05)."""
+        """Five-qubit fused blocks on the tensor cores (tcgen05; the default)
+        or, with False, on the CUDA cores."""
         _check(self.L.qslc_set_fusion_tc(self.h, int(on)))
 
     def fused_blocks(self) -> int:

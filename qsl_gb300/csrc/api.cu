@@ -277,7 +277,10 @@ int qslc_clone(const qslc_state *src, qslc_state **out)
     s->resizable = src->resizable;
     if (src->np) rc = np_set_weight(s, src->nones);
     else rc = alloc_amps(s, src->namps);
-    if (!rc) s->fuse_k = src->fuse_k;
+    if (!rc) {
+        s->fuse_k = src->fuse_k;
+        s->fuse_tc = src->fuse_tc;
+    }
     if (!rc) {
         cudaStreamSynchronize(src->stream);
         cudaError_t e = cudaMemcpyAsync(s->amps, src->amps, src->namps * src->amp_bytes(),

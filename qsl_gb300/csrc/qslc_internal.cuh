@@ -113,7 +113,7 @@ struct qslc_state {
     qslc::NPTables *npt = nullptr;
     // precision form (fused.cu): queued gates, fusion width, block matrices
     unsigned fuse_k = 0;
-    int fuse_tc = 0;          // five-qubit blocks on the tensor cores (fused_tc.cu)
+    int fuse_tc = 1;          // five-qubit blocks on the tensor cores (fused_tc.cu)
     std::vector<qslc::GateOp> fuse_queue;
     qslc::Scratch fuse_mats;
     qslc::Scratch fuse_tc_mats;   // packed tensor-core operands, then an error word

@@ -239,6 +239,28 @@ def case_resize(seed, n0, steps, fp32):
                 states=np.concatenate(states), probs=probs, u=u, keys=keys, counts=counts)
 
 
+def results_table():
+    """A table written by the reference's own Results::writeToFile
+    (include/qsl/benchmark/results.tpp:315-355), with values that exercise
+    the default float format: tiny, huge, exact, long mantissas."""
+    rng = np.random.default_rng(77)
+    heads = ["nones", "nqubits", "Default", "Default+OMP", "Cuda", "CudaNP"]
+    meta = ["Testing the phase gate", "Results are in seconds"]
+    ints = np.array([[w, 16] for w in range(1, 16)], dtype=np.uint32)
+    fps = np.concatenate([rng.uniform(1e-6, 1e-4, (15, 2)), 10.0 ** rng.uniform(-9, 9, (15, 2))],
+                         axis=1)
+    fps[0, :] = [0.1, 1.0, 123456789.0, 1e-7]
+    fps[1, :] = [5.11879e-05, 0.0, 100000.0, 999999.5]
+    path = os.path.join(HERE, "results_ref.txt")
+    rc = oracle.ref_lib().qslref_results_write(path.encode(), "\n".join(heads).encode(),
+                                               "\n".join(meta).encode(), 15, 2, ints.ctypes.data, 4,
+                                               np.ascontiguousarray(fps).ctypes.data)
+    assert rc == 0
+    with open(os.path.join(HERE, "results_ref.json"), "w") as f:
+        json.dump({"headings": heads, "meta": meta, "ints": ints.tolist(),
+                   "fps": [[float(x).hex() for x in row] for row in fps]}, f, indent=0)
+
+
 def kats():
     lib = oracle.ref_lib()
     seq = [0b111]
@@ -275,6 +297,7 @@ def main():
                             **{f"{k}__{f}": v for k, c in cases.items() for f, v in c.items()})
     lay = case_layered(2021, 12, 20, 10000)
     np.savez_compressed(os.path.join(HERE, "layered_n12.npz"), **lay)
+    results_table()
     with open(os.path.join(HERE, "kat.json"), "w") as f:
         json.dump(kats(), f, indent=0, sort_keys=True)
     print("fixtures written to", HERE)

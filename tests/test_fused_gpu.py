@@ -27,14 +27,15 @@ def random_circuit(rng, n, length):
     return circ
 
 
-@pytest.mark.parametrize("k", [2, 3, 4, 5])
-def test_fused_matches_fp64(qsl, port, k):
+@pytest.mark.parametrize("k,tc", [(2, False), (3, False), (4, False), (5, False), (5, True)])
+def test_fused_matches_fp64(qsl, port, k, tc):
     from qsl_gb300 import workloads
     rng = np.random.default_rng(40 + k)
     n = 14
     circ = random_circuit(rng, n, 400) + workloads.layered_mixed(n, 6, 5 + k)
     gpu = qsl.Qubits(n, dtype=np.complex64)
     gpu.set_fusion(k)
+    gpu.set_fusion_tc(tc)
     workloads.apply(gpu, circ)
     ref = port.PortQubits(n)
     workloads.apply(ref, circ)
