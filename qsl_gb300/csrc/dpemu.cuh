@@ -84,6 +84,7 @@ struct MulConst {
     int e;           // unbiased exponent
     uint64_t sign;   // SIGN or 0
     int usable;      // 0: zero/subnormal/inf/nan -- always use the native path
+    uint32_t m0, m1; // m split into its low 32 and high 21 bits
 };
 
 inline MulConst make_const(double c)
@@ -96,6 +97,8 @@ inline MulConst make_const(double c)
     k.usable = (ef != 0 && ef != 0x7FF) ? 1 : 0;
     k.m = (b & MANT) | HIDDEN;
     k.e = ef - 1023;
+    k.m0 = uint32_t(k.m);
+    k.m1 = uint32_t(k.m >> 32);
     return k;
 }
 
@@ -251,14 +254,105 @@ QSLC_HD uint64_t div_rn(uint64_t x, const DivConst &y, bool &ok)
     return sign | (uint64_t(e + 1023) << 52) | (t & MANT);
 }
 
-// RN(RN(a*c) + RN(b*s)): the shape of every rotation output in qsl's gate
-// loops (e.g. a0.real*cos + a1.imag*sin, gates.cpp:139).  `ok` reports
-// whether the integer path covered every step.
-QSLC_HD uint64_t dot2_rn(uint64_t a, const MulConst &c, uint64_t b, const MulConst &s, bool &ok)
+// ---------------------------------------------------------------------------
+// The dot-product path.  A rounded product stays unpacked -- sign, exponent,
+// 53-bit significand -- and goes straight into the sum, so no product is
+// packed into IEEE bits and unpacked again.  The product is built from four
+// 32 x 32 -> 64 partial products, and every shift is by a constant; the sum
+// normalises add and subtract the same way, without branches on the signs.
+// ---------------------------------------------------------------------------
+
+// value = m * 2^(e - 52) with m in [2^52, 2^53), or zero when m == 0
+struct Unp {
+    uint64_t m;
+    int e;
+    uint64_t sign;   // SIGN or 0
+};
+
+// RN(a * c), unpacked.  Declines (ok = false) a subnormal, infinite or NaN
+// operand and a product outside the normal range.
+QSLC_HD Unp mul_unp(uint64_t a, const MulConst &c, bool &ok)
 {
-    const uint64_t p = mul_rn(a, c, ok);
-    const uint64_t q = mul_rn(b, s, ok);
-    return add_rn(p, q, ok);
+    Unp r;
+    r.sign = (a ^ c.sign) & SIGN;
+    const uint32_t ahi = uint32_t(a >> 32), alo = uint32_t(a);
+    if (((ahi & 0x7FFFFFFFu) | alo) == 0) {        // +-0 * c
+        r.m = 0;
+        r.e = 0;
+        return r;
+    }
+    const int ef = int((ahi >> 20) & 0x7FF);
+    ok = ok & (ef != 0) & (ef != 0x7FF);
+    const uint32_t a1 = (ahi & 0xFFFFFu) | 0x100000u;
+    const uint64_t p00 = uint64_t(alo) * c.m0, p01 = uint64_t(alo) * c.m1;
+    const uint64_t p10 = uint64_t(a1) * c.m0, p11 = uint64_t(a1) * c.m1;
+    const uint64_t mid = p01 + p10;                 // < 2^54
+    const uint64_t lo = p00 + (mid << 32);
+    const uint64_t hi = p11 + (mid >> 32) + uint64_t(lo < p00);   // product = hi:lo < 2^106
+    const uint64_t top = hi >> 41;                  // leading bit at 105 (else at 104)
+    uint64_t q = (hi << 13) | (lo >> 51);           // product >> 51
+    uint64_t st = uint64_t((lo & ((uint64_t(1) << 51) - 1)) != 0);
+    st |= q & top;                                  // with the lead at 105, bit 51 is sticky too
+    q >>= top;
+    uint64_t m = q >> 1;
+    m += (q & 1) & (st | (m & 1));                  // round to nearest even
+    int e = ef - 1023 + c.e + int(top);
+    const uint64_t carry = m >> 53;
+    m >>= carry;
+    e += int(carry);
+    ok = ok & (e >= -1022) & (e <= 1023);
+    r.m = m;
+    r.e = e;
+    return r;
+}
+
+// RN(x + y) of two unpacked values, packed into IEEE bits.
+QSLC_HD uint64_t add_unp(Unp x, Unp y, bool &ok)
+{
+    const uint64_t kx = x.m ? (uint64_t(x.e + 1100) << 53) | x.m : 0;
+    const uint64_t ky = y.m ? (uint64_t(y.e + 1100) << 53) | y.m : 0;
+    if (kx < ky) {
+        const Unp t = x;
+        x = y;
+        y = t;
+    }
+    const uint64_t X = x.m << 10, Yf = y.m << 10;   // lead bit at 62, 10 guard bits
+    int d = x.e - y.e;
+    d = d < 0 ? 0 : (d > 63 ? 63 : d);              // d < 0 only when y is zero
+    const uint64_t Y = (Yf >> d) | uint64_t((Yf & ((uint64_t(1) << d) - 1)) != 0);
+    const bool sub = (x.sign ^ y.sign) != 0;
+    uint64_t S = sub ? X - Y : X + Y;
+    if (S == 0) return sub ? 0 : (x.sign & y.sign); // exact cancellation: +0; 0 + 0 keeps a shared sign
+    const int lz = clz64(S);
+    int e = x.e;
+    if (lz == 0) {                                  // carry out of an addition
+        S = (S >> 1) | (S & 1);
+        e += 1;
+    } else {
+        S <<= (lz - 1);
+        e -= lz - 1;
+    }
+    uint64_t m = S >> 10;
+    const uint64_t rb = S & 0x3FF;
+    m += uint64_t(rb > 0x200) | (uint64_t(rb == 0x200) & (m & 1));
+    const uint64_t carry = m >> 53;
+    m >>= carry;
+    e += int(carry);
+    ok = ok & (e >= -1022) & (e <= 1023);
+    return x.sign | (uint64_t(e + 1023) << 52) | (m & MANT);
+}
+
+// RN(RN(a*c) + RN(b*s)), or RN(RN(a*c) - RN(b*s)) when neg: the shape of
+// every rotation and phase output in qsl's gate loops (e.g. a0.real*cos +
+// a1.imag*sin, gates.cpp:139).  `ok` reports whether the integer path
+// covered every step; when it did not, the result is meaningless.
+QSLC_HD uint64_t dot2_rn(uint64_t a, const MulConst &c, uint64_t b, const MulConst &s, bool neg,
+                         bool &ok)
+{
+    const Unp p = mul_unp(a, c, ok);
+    Unp q = mul_unp(b, s, ok);
+    if (neg) q.sign ^= SIGN;
+    return add_unp(p, q, ok);
 }
 
 }  // namespace emu

@@ -61,10 +61,7 @@ __device__ __forceinline__ T dot2(T a, T k1, const emu::MulConst &e1, T b, T k2,
     if constexpr (EMU && sizeof(T) == 8) {
         bool ok = (e1.usable & e2.usable) != 0;
         if (ok) {
-            uint64_t p = emu::mul_rn(emu::dbits(a), e1, ok);
-            uint64_t q = emu::mul_rn(emu::dbits(b), e2, ok);
-            if (NEG) q ^= emu::SIGN;
-            uint64_t r = emu::add_rn(p, q, ok);
+            const uint64_t r = emu::dot2_rn(emu::dbits(a), e1, emu::dbits(b), e2, NEG, ok);
             if (ok) return emu::dfrom(r);
         }
     }

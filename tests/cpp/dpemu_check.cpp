@@ -30,7 +30,7 @@ static double make(int emin, int emax)
 int main(int argc, char **argv)
 {
     const long N = argc > 1 ? std::atol(argv[1]) : 20000000;
-    long fails = 0, declined_mul = 0, declined_add = 0;
+    long fails = 0, declined_mul = 0, declined_add = 0, declined_dot = 0;
     for (long i = 0; i < N; i++) {
         // multiply: constant-like c, amplitude-like a, plus edge exponents
         double c = (i & 7) == 0 ? make(-1022, 1023) : make(-6, 1);
@@ -87,21 +87,38 @@ int main(int argc, char **argv)
                 if (fails++ < 10) std::printf("div2 %a / %a: got %a want %a\n", prod, yv, dfrom(qd), (double)qref2);
             }
         }
-        // the fused shape of a rotation output
-        double b = make(-80, 2), sn = make(-6, 1);
-        MulConst ks = make_const(sn);
-        ok = true;
-        uint64_t d = dot2_rn(dbits(a), k, dbits(b), ks, ok);
-        volatile double p1 = a * c, p2 = b * sn;
-        volatile double dref = p1 + p2;
-        if (ok && d != dbits(dref)) {
-            if (fails++ < 10) std::printf("dot2 mismatch\n");
+        // the fused shape of a rotation output, RN(RN(a*c) +- RN(b*s)), with
+        // the operand mixes a gate sees: amplitude-like values, zeros,
+        // near-cancellation (b*s close to a*c), wide exponent gaps
+        for (int rep = 0; rep < 2; rep++) {
+            double a2 = make(-80, 2), c2 = make(-6, 1), b2 = make(-80, 2), s2 = make(-6, 1);
+            const int kind = int(rng() % 8);
+            if (kind == 0) a2 = (rng() & 1) ? 0.0 : -0.0;
+            if (kind == 1) b2 = (rng() & 1) ? 0.0 : -0.0;
+            if (kind == 2) { a2 = (rng() & 1) ? 0.0 : -0.0; b2 = (rng() & 1) ? 0.0 : -0.0; }
+            if (kind == 3) { b2 = a2; s2 = c2; }                                  // exact cancellation
+            if (kind == 4) { b2 = dfrom(dbits(a2) + (rng() % 5) - 2); s2 = c2; }   // near cancellation
+            if (kind == 5) { b2 = make(-1022, -900); }                             // tiny second term
+            if (kind == 6 && (i & 63) == 0) { a2 = make(-1074 + 53, -1000); c2 = make(-60, -20); }  // underflow edge
+            const bool neg = rng() & 1;
+            MulConst kc2 = make_const(c2), ks2 = make_const(s2);
+            ok = (kc2.usable & ks2.usable) != 0;
+            uint64_t d = dot2_rn(dbits(a2), kc2, dbits(b2), ks2, neg, ok);
+            volatile double p1 = a2 * c2, p2 = b2 * s2;
+            volatile double dref = neg ? p1 - p2 : p1 + p2;
+            if (ok && d != dbits(dref)) {
+                if (fails++ < 10)
+                    std::printf("dot2 %a*%a %c %a*%a: got %a want %a\n", a2, c2, neg ? '-' : '+', b2, s2,
+                                dfrom(d), (double)dref);
+            }
+            if (!ok) declined_dot++;
         }
     }
-    std::printf("cases %ld fails %ld declined mul %ld add %ld\n", N, fails, declined_mul, declined_add);
+    std::printf("cases %ld fails %ld declined mul %ld add %ld dot2 %ld\n", N, fails, declined_mul,
+                declined_add, declined_dot);
     if (fails) return 1;
     // declines must be rare on amplitude-like data
-    if (declined_add > N / 100) return 2;
+    if (declined_add > N / 100 || declined_dot > N / 50) return 2;
     std::puts("dpemu ok");
     return 0;
 }

@@ -1,0 +1,64 @@
+"""Every split of the dense gate arithmetic between the FP64 pipe and the
+integer-pipe binary64 emulation gives the oracle's bits.
+
+QSLC_EMU_MASK selects which of the four outputs of an amplitude pair (and
+QSLC_EMU_MASK_DIAG which of the two outputs of a diagonal update) the
+integer pipes compute; the library reads them once per process, so each
+setting runs in its own process."""
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import bits, random_state
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+DENSE = ("hadamard", "rotateX", "rotateY", "rotateZ", "phase", "controlRotateX",
+         "controlRotateY", "controlRotateZ", "controlPhase", "controlHadamard", "npRotateX",
+         "npRotateY", "npHadamard")
+
+SCRIPT = r"""
+import sys, numpy as np
+sys.path.insert(0, {root!r})
+import qsl_gb300 as q
+d = np.load({inp!r})
+sim = q.Qubits(state=d["state"])
+for g, a, b, x in zip(d["names"], d["q1"], d["q2"], d["ang"]):
+    sim.gate(str(g), int(a), None if int(b) < 0 else int(b), float(x))
+np.save({out!r}, sim.getState())
+"""
+
+
+def circuit(rng, n, reps):
+    names, q1, q2, ang = [], [], [], []
+    for _ in range(reps):
+        for g in DENSE:
+            a, b = (int(v) for v in rng.choice(n, 2, replace=False))
+            two = g.startswith(("control", "np"))
+            names.append(g)
+            q1.append(a)
+            q2.append(b if two else -1)
+            ang.append(float(rng.uniform(0, 2 * np.pi)))
+    return np.array(names), np.array(q1), np.array(q2), np.array(ang)
+
+
+@pytest.mark.parametrize("pair,diag", [(0, 0), (1, 2), (3, 1), (5, 3), (7, 1), (15, 3)])
+def test_every_emulation_split_is_exact(qsl, port, tmp_path, pair, diag):
+    rng = np.random.default_rng(pair * 7 + diag)
+    n = 12
+    st = random_state(rng, n)
+    names, q1, q2, ang = circuit(rng, n, 6)
+    inp, out = str(tmp_path / "in.npz"), str(tmp_path / "out.npy")
+    np.savez(inp, state=st, names=names, q1=q1, q2=q2, ang=ang)
+    env = dict(os.environ, QSLC_EMU_MASK=str(pair), QSLC_EMU_MASK_DIAG=str(diag))
+    r = subprocess.run([sys.executable, "-c", SCRIPT.format(root=ROOT, inp=inp, out=out)],
+                       env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    cpu = port.PortQubits(n, state=st)
+    for g, a, b, x in zip(names, q1, q2, ang):
+        cpu.gate(str(g), int(a), None if int(b) < 0 else int(b), float(x))
+    assert np.array_equal(bits(np.load(out)), bits(cpu.state))
