@@ -306,8 +306,32 @@ QSLC_HD Unp mul_unp(uint64_t a, const MulConst &c, bool &ok)
     return r;
 }
 
-// RN(x + y) of two unpacked values, packed into IEEE bits.
-QSLC_HD uint64_t add_unp(Unp x, Unp y, bool &ok)
+// IEEE bits to the unpacked form; declines subnormals, infinities, NaNs.
+QSLC_HD Unp unpack(uint64_t a, bool &ok)
+{
+    Unp r;
+    r.sign = a & SIGN;
+    const uint32_t ahi = uint32_t(a >> 32);
+    const int ef = int((ahi >> 20) & 0x7FF);
+    if (((ahi & 0x7FFFFFFFu) | uint32_t(a)) == 0) {
+        r.m = 0;
+        r.e = 0;
+        return r;
+    }
+    ok = ok & (ef != 0) & (ef != 0x7FF);
+    r.m = (a & MANT) | HIDDEN;
+    r.e = ef - 1023;
+    return r;
+}
+
+QSLC_HD uint64_t pack(const Unp &x)
+{
+    if (x.m == 0) return x.sign;
+    return x.sign | (uint64_t(x.e + 1023) << 52) | (x.m & MANT);
+}
+
+// RN(x + y) of two unpacked values, still unpacked (a zero keeps its sign).
+QSLC_HD Unp add_core(Unp x, Unp y, bool &ok)
 {
     const uint64_t kx = x.m ? (uint64_t(x.e + 1100) << 53) | x.m : 0;
     const uint64_t ky = y.m ? (uint64_t(y.e + 1100) << 53) | y.m : 0;
@@ -322,7 +346,13 @@ QSLC_HD uint64_t add_unp(Unp x, Unp y, bool &ok)
     const uint64_t Y = (Yf >> d) | uint64_t((Yf & ((uint64_t(1) << d) - 1)) != 0);
     const bool sub = (x.sign ^ y.sign) != 0;
     uint64_t S = sub ? X - Y : X + Y;
-    if (S == 0) return sub ? 0 : (x.sign & y.sign); // exact cancellation: +0; 0 + 0 keeps a shared sign
+    Unp r;
+    if (S == 0) {                                   // exact cancellation: +0; 0 + 0 keeps a shared sign
+        r.m = 0;
+        r.e = 0;
+        r.sign = sub ? 0 : (x.sign & y.sign);
+        return r;
+    }
     const int lz = clz64(S);
     int e = x.e;
     if (lz == 0) {                                  // carry out of an addition
@@ -339,7 +369,54 @@ QSLC_HD uint64_t add_unp(Unp x, Unp y, bool &ok)
     m >>= carry;
     e += int(carry);
     ok = ok & (e >= -1022) & (e <= 1023);
-    return x.sign | (uint64_t(e + 1023) << 52) | (m & MANT);
+    r.m = m;
+    r.e = e;
+    r.sign = x.sign;
+    return r;
+}
+
+// RN(x + y) of two unpacked values, packed into IEEE bits.
+QSLC_HD uint64_t add_unp(const Unp &x, const Unp &y, bool &ok) { return pack(add_core(x, y, ok)); }
+
+// RN(x / y) for an unpacked x and a normal constant y, packed.  The
+// quotient significand t = floor(mx * 2^k / my) (k = 52 when mx >= my, else
+// 53, so that t has 53 bits) is estimated from the high part of mx times the
+// 64-bit reciprocal, leaving out the low 32 x 32 partial product; the
+// estimate is then low by at most three (one from the reciprocal, two from
+// the dropped part when k = 53).  The exact remainder
+// r = mx * 2^k - t * my (its low 64 bits are all of it) corrects it, and
+// comparing 2r with my rounds to nearest even.
+QSLC_HD uint64_t div_unp(const Unp &x, const DivConst &y, bool &ok)
+{
+    const uint64_t sign = x.sign ^ y.sign;
+    if (x.m == 0) return sign;
+    const uint64_t mx = x.m;
+    const uint32_t m0 = uint32_t(mx), m1 = uint32_t(mx >> 32);
+    const uint32_t r0 = uint32_t(y.rinv), r1 = uint32_t(y.rinv >> 32);
+    const uint64_t a = uint64_t(m0) * r1, b = uint64_t(m1) * r0;
+    const uint64_t mid = a + b;
+    const uint64_t midc = uint64_t(mid < a);       // carry out of the 64-bit sum
+    const uint64_t hi = uint64_t(m1) * r1 + (mid >> 32) + (midc << 32);
+    const uint64_t k53 = uint64_t(mx < y.m);
+    uint64_t t = (hi << k53) | ((mid >> 31) & k53);  // bit 63 of the truncated product is bit 31 of mid
+    uint64_t r = (mx << (52 + k53)) - t * y.m;
+    const uint64_t c1 = uint64_t(r >= y.m);
+    t += c1;
+    r -= c1 * y.m;
+    const uint64_t c2 = uint64_t(r >= y.m);
+    t += c2;
+    r -= c2 * y.m;
+    const uint64_t c3 = uint64_t(r >= y.m);
+    t += c3;
+    r -= c3 * y.m;
+    const uint64_t r2 = r << 1;
+    t += uint64_t(r2 > y.m) | (uint64_t(r2 == y.m) & (t & 1));
+    int e = x.e - y.e - int(k53);
+    const uint64_t carry = t >> 53;
+    t >>= carry;
+    e += int(carry);
+    ok = ok & (e >= -1022) & (e <= 1023);
+    return sign | (uint64_t(e + 1023) << 52) | (t & MANT);
 }
 
 // RN(RN(a*c) + RN(b*s)), or RN(RN(a*c) - RN(b*s)) when neg: the shape of

@@ -33,17 +33,23 @@ struct Coef {
 // One Hadamard output, RN(RN(a +- b) / sqrt2) (gates.cpp:95-98).  The
 // division always runs on the integer pipes (an FP64 divide is a long
 // iteration on the FP64 pipe); with EMU the sum does too.
-template <class T, bool EMU, bool NEG>
-__device__ __forceinline__ T hdiv(T a, T b, const Coef<T> &k)
+template <class T, bool NEG>
+__device__ __forceinline__ T hdiv(bool em, T a, T b, const Coef<T> &k)
 {
     using R = rn<T>;
     if constexpr (sizeof(T) == 8) {
         bool ok = k.kd.usable != 0;
         if (ok) {
-            uint64_t sb;
-            if constexpr (EMU) sb = emu::add_rn(emu::dbits(a), emu::dbits(b) ^ (NEG ? emu::SIGN : 0), ok);
-            else sb = emu::dbits(NEG ? R::sub(a, b) : R::add(a, b));
-            const uint64_t q = emu::div_rn(sb, k.kd, ok);
+            emu::Unp sum;
+            if (em) {
+                const emu::Unp x = emu::unpack(emu::dbits(a), ok);
+                emu::Unp y = emu::unpack(emu::dbits(b), ok);
+                if (NEG) y.sign ^= emu::SIGN;
+                sum = emu::add_core(x, y, ok);
+            } else {
+                sum = emu::unpack(emu::dbits(NEG ? R::sub(a, b) : R::add(a, b)), ok);
+            }
+            const uint64_t q = emu::div_unp(sum, k.kd, ok);
             if (ok) return emu::dfrom(q);
         }
     }
@@ -54,12 +60,12 @@ __device__ __forceinline__ T hdiv(T a, T b, const Coef<T> &k)
 // RN(RN(a*k1) - RN(b*k2)) when NEG.  With EMU the integer pipes compute it
 // (dpemu.cuh), falling back to the FP64 pipe for operands the integer path
 // declines; either way the bits are the reference's.
-template <class T, bool EMU, bool NEG>
-__device__ __forceinline__ T dot2(T a, T k1, const emu::MulConst &e1, T b, T k2,
+template <class T, bool NEG>
+__device__ __forceinline__ T dot2(bool em, T a, T k1, const emu::MulConst &e1, T b, T k2,
                                   const emu::MulConst &e2)
 {
-    if constexpr (EMU && sizeof(T) == 8) {
-        bool ok = (e1.usable & e2.usable) != 0;
+    if constexpr (sizeof(T) == 8) {
+        bool ok = em && (e1.usable & e2.usable) != 0;
         if (ok) {
             const uint64_t r = emu::dot2_rn(emu::dbits(a), e1, emu::dbits(b), e2, NEG, ok);
             if (ok) return emu::dfrom(r);
@@ -69,13 +75,14 @@ __device__ __forceinline__ T dot2(T a, T k1, const emu::MulConst &e1, T b, T k2,
     return NEG ? R::sub(R::mul(a, k1), R::mul(b, k2)) : R::add(R::mul(a, k1), R::mul(b, k2));
 }
 
-// EM: bit i set = output i (r0.x, r0.y, r1.x, r1.y) on the integer pipes.
-template <class T, int OP, int EM = 0>
-__device__ __forceinline__ void pair_update(cplx<T> &a0, cplx<T> &a1, const Coef<T> &k)
+// em: bit i set = output i (r0.x, r0.y, r1.x, r1.y) on the integer pipes;
+// it must be the same across a warp.
+template <class T, int OP>
+__device__ __forceinline__ void pair_update(cplx<T> &a0, cplx<T> &a1, const Coef<T> &k, unsigned em = 0)
 {
     using R = rn<T>;
     cplx<T> r0, r1;
-    constexpr bool E0 = EM & 1, E1 = EM & 2, E2 = EM & 4, E3 = EM & 8;
+    const bool E0 = em & 1, E1 = em & 2, E2 = em & 4, E3 = em & 8;
     if constexpr (OP == P_SWAP) {            // gates.cpp:41, :236, :524
         r0 = a1;
         r1 = a0;
@@ -83,32 +90,32 @@ __device__ __forceinline__ void pair_update(cplx<T> &a0, cplx<T> &a1, const Coef
         r0.x = a1.y; r0.y = -a1.x;
         r1.x = -a0.y; r1.y = a0.x;
     } else if constexpr (OP == P_H) {        // gates.cpp:95-98, :493-496, :675-678
-        r0.x = hdiv<T, E0, false>(a0.x, a1.x, k);
-        r0.y = hdiv<T, E1, false>(a0.y, a1.y, k);
-        r1.x = hdiv<T, E2, true>(a0.x, a1.x, k);
-        r1.y = hdiv<T, E3, true>(a0.y, a1.y, k);
+        r0.x = hdiv<T, false>(E0, a0.x, a1.x, k);
+        r0.y = hdiv<T, false>(E1, a0.y, a1.y, k);
+        r1.x = hdiv<T, true>(E2, a0.x, a1.x, k);
+        r1.y = hdiv<T, true>(E3, a0.y, a1.y, k);
     } else if constexpr (OP == P_RX) {       // gates.cpp:139-144, :336-341, :595-600
-        r0.x = dot2<T, E0, false>(a0.x, k.c, k.kc, a1.y, k.s, k.ks);
-        r0.y = dot2<T, E1, true>(a0.y, k.c, k.kc, a1.x, k.s, k.ks);
-        r1.x = dot2<T, E2, false>(a1.x, k.c, k.kc, a0.y, k.s, k.ks);
-        r1.y = dot2<T, E3, true>(a1.y, k.c, k.kc, a0.x, k.s, k.ks);
+        r0.x = dot2<T, false>(E0, a0.x, k.c, k.kc, a1.y, k.s, k.ks);
+        r0.y = dot2<T, true>(E1, a0.y, k.c, k.kc, a1.x, k.s, k.ks);
+        r1.x = dot2<T, false>(E2, a1.x, k.c, k.kc, a0.y, k.s, k.ks);
+        r1.y = dot2<T, true>(E3, a1.y, k.c, k.kc, a0.x, k.s, k.ks);
     } else if constexpr (OP == P_RY) {       // gates.cpp:169-174, :380-385, :638-643
-        r0.x = dot2<T, E0, true>(a0.x, k.c, k.kc, a1.x, k.s, k.ks);
-        r0.y = dot2<T, E1, true>(a0.y, k.c, k.kc, a1.y, k.s, k.ks);
-        r1.x = dot2<T, E2, false>(a0.x, k.s, k.ks, a1.x, k.c, k.kc);
-        r1.y = dot2<T, E3, false>(a0.y, k.s, k.ks, a1.y, k.c, k.kc);
+        r0.x = dot2<T, true>(E0, a0.x, k.c, k.kc, a1.x, k.s, k.ks);
+        r0.y = dot2<T, true>(E1, a0.y, k.c, k.kc, a1.y, k.s, k.ks);
+        r1.x = dot2<T, false>(E2, a0.x, k.s, k.ks, a1.x, k.c, k.kc);
+        r1.y = dot2<T, false>(E3, a0.y, k.s, k.ks, a1.y, k.c, k.kc);
     } else {                                 // P_RZ: gates.cpp:200-205, :424-429
-        r0.x = dot2<T, E0, false>(a0.x, k.c, k.kc, a0.y, k.s, k.ks);
-        r0.y = dot2<T, E1, true>(a0.y, k.c, k.kc, a0.x, k.s, k.ks);
-        r1.x = dot2<T, E2, true>(a1.x, k.c, k.kc, a1.y, k.s, k.ks);
-        r1.y = dot2<T, E3, false>(a1.y, k.c, k.kc, a1.x, k.s, k.ks);
+        r0.x = dot2<T, false>(E0, a0.x, k.c, k.kc, a0.y, k.s, k.ks);
+        r0.y = dot2<T, true>(E1, a0.y, k.c, k.kc, a0.x, k.s, k.ks);
+        r1.x = dot2<T, true>(E2, a1.x, k.c, k.kc, a1.y, k.s, k.ks);
+        r1.y = dot2<T, false>(E3, a1.y, k.c, k.kc, a1.x, k.s, k.ks);
     }
     a0 = r0;
     a1 = r1;
 }
 
-template <class T, int OP, int EM = 0>
-__device__ __forceinline__ void diag_update(cplx<T> &a, const Coef<T> &k)
+template <class T, int OP>
+__device__ __forceinline__ void diag_update(cplx<T> &a, const Coef<T> &k, unsigned em = 0)
 {
     using R = rn<T>;
     if constexpr (OP == D_NEG) {             // gates.cpp:76-77, :296-297 (x *= -1)
@@ -116,39 +123,70 @@ __device__ __forceinline__ void diag_update(cplx<T> &a, const Coef<T> &k)
         a.y = R::mul(a.y, T(-1));
     } else {                                 // gates.cpp:114-115, :460-461
         T x = a.x, y = a.y;
-        a.x = dot2<T, (EM & 1) != 0, true>(x, k.c, k.kc, y, k.s, k.ks);
-        a.y = dot2<T, (EM & 2) != 0, false>(y, k.c, k.kc, x, k.s, k.ks);
+        a.x = dot2<T, true>((em & 1) != 0, x, k.c, k.kc, y, k.s, k.ks);
+        a.y = dot2<T, false>((em & 2) != 0, y, k.c, k.kc, x, k.s, k.ks);
     }
 }
 
+// The sweeps below take ITEMS work items per grid-stride iteration (at j,
+// j + stride, j + 2 stride), all loads first.  `pat` holds one emulation
+// mask per item, 4 bits each: item r uses (pat >> 4r) & 15, so the share of
+// outputs computed on the integer pipes can be set in steps of one output
+// in twelve (pair gates) or one in six (diagonal gates).  Masks differ only
+// between items, never between threads of a warp.
+constexpr int ITEMS = 3;
+
 // One-qubit pair gates: pairs (i0, i0 + 2^t), i0 = insert0(j, t).
-template <class T, int OP, int EM = 0>
+template <class T, int OP>
 __global__ void __launch_bounds__(256) k_pair1(cplx<T> *__restrict__ st, uint64_t npairs,
-                                               unsigned t, Coef<T> k)
+                                               unsigned t, Coef<T> k, unsigned pat)
 {
     const uint64_t bit = uint64_t(1) << t;
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
-    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < npairs; j += stride) {
-        uint64_t i0 = insert0(j, t);
-        cplx<T> a0 = st[i0], a1 = st[i0 | bit];
-        pair_update<T, OP, EM>(a0, a1, k);
-        st[i0] = a0;
-        st[i0 | bit] = a1;
+    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < npairs; j += ITEMS * stride) {
+        cplx<T> a0[ITEMS], a1[ITEMS];
+        uint64_t i0[ITEMS];
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++) {
+            i0[r] = insert0(j + r * stride, t);
+            if (j + r * stride < npairs) {
+                a0[r] = st[i0[r]];
+                a1[r] = st[i0[r] | bit];
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++) {
+            if (j + r * stride < npairs) {
+                pair_update<T, OP>(a0[r], a1[r], k, (pat >> (4 * r)) & 15);
+                st[i0[r]] = a0[r];
+                st[i0[r] | bit] = a1[r];
+            }
+        }
     }
 }
 
 // One-qubit diagonal gates on the |1> half: index insert0(j, t) | 2^t.
-template <class T, int OP, int EM = 0>
+template <class T, int OP>
 __global__ void __launch_bounds__(256) k_diag1(cplx<T> *__restrict__ st, uint64_t count,
-                                               unsigned t, Coef<T> k)
+                                               unsigned t, Coef<T> k, unsigned pat)
 {
     const uint64_t bit = uint64_t(1) << t;
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
-    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < count; j += stride) {
-        uint64_t i = insert0(j, t) | bit;
-        cplx<T> a = st[i];
-        diag_update<T, OP, EM>(a, k);
-        st[i] = a;
+    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < count; j += ITEMS * stride) {
+        cplx<T> a[ITEMS];
+        uint64_t i[ITEMS];
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++) {
+            i[r] = insert0(j + r * stride, t) | bit;
+            if (j + r * stride < count) a[r] = st[i[r]];
+        }
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++) {
+            if (j + r * stride < count) {
+                diag_update<T, OP>(a[r], k, (pat >> (4 * r)) & 3);
+                st[i[r]] = a[r];
+            }
+        }
     }
 }
 
@@ -159,41 +197,64 @@ __global__ void __launch_bounds__(256) k_diag1(cplx<T> *__restrict__ st, uint64_
 // MODE 0: controlled pair (base|b1, base|b1|b2), b1 = control bit;
 // MODE 1: number-preserving pair (base|b1, base|b2);
 // MODE 2: fswap = MODE 1 swap plus negation of base|b1|b2.
-template <class T, int OP, int MODE, int EM = 0>
+template <class T, int OP, int MODE>
 __global__ void __launch_bounds__(256) k_pair2(cplx<T> *__restrict__ st, uint64_t nquads,
                                                unsigned lo, unsigned hi, uint64_t b1,
-                                               uint64_t b2, Coef<T> k)
+                                               uint64_t b2, Coef<T> k, unsigned pat)
 {
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
-    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < nquads; j += stride) {
-        uint64_t base = insert00(j, lo, hi);
-        uint64_t x1 = base | b1;
-        uint64_t x2 = (MODE == 0) ? (x1 | b2) : (base | b2);
-        cplx<T> a0 = st[x1], a1 = st[x2];
-        pair_update<T, OP, EM>(a0, a1, k);
-        st[x1] = a0;
-        st[x2] = a1;
-        if constexpr (MODE == 2) {
-            uint64_t x3 = base | b1 | b2;
-            cplx<T> a = st[x3];
-            diag_update<T, D_NEG>(a, k);
-            st[x3] = a;
+    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < nquads; j += ITEMS * stride) {
+        cplx<T> a0[ITEMS], a1[ITEMS];
+        uint64_t x1[ITEMS], x2[ITEMS];
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++) {
+            const uint64_t base = insert00(j + r * stride, lo, hi);
+            x1[r] = base | b1;
+            x2[r] = (MODE == 0) ? (x1[r] | b2) : (base | b2);
+            if (j + r * stride < nquads) {
+                a0[r] = st[x1[r]];
+                a1[r] = st[x2[r]];
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++) {
+            if (j + r * stride < nquads) {
+                pair_update<T, OP>(a0[r], a1[r], k, (pat >> (4 * r)) & 15);
+                st[x1[r]] = a0[r];
+                st[x2[r]] = a1[r];
+                if constexpr (MODE == 2) {
+                    const uint64_t x3 = x1[r] | b2;
+                    cplx<T> a = st[x3];
+                    diag_update<T, D_NEG>(a, k);
+                    st[x3] = a;
+                }
+            }
         }
     }
 }
 
 // controlZ / controlPhase: the |11> quarter (gates.cpp:277-301, :436-465).
-template <class T, int OP, int EM = 0>
+template <class T, int OP>
 __global__ void __launch_bounds__(256) k_diag2(cplx<T> *__restrict__ st, uint64_t nquads,
                                                unsigned lo, unsigned hi, uint64_t both,
-                                               Coef<T> k)
+                                               Coef<T> k, unsigned pat)
 {
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
-    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < nquads; j += stride) {
-        uint64_t i = insert00(j, lo, hi) | both;
-        cplx<T> a = st[i];
-        diag_update<T, OP, EM>(a, k);
-        st[i] = a;
+    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < nquads; j += ITEMS * stride) {
+        cplx<T> a[ITEMS];
+        uint64_t i[ITEMS];
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++) {
+            i[r] = insert00(j + r * stride, lo, hi) | both;
+            if (j + r * stride < nquads) a[r] = st[i[r]];
+        }
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++) {
+            if (j + r * stride < nquads) {
+                diag_update<T, OP>(a[r], k, (pat >> (4 * r)) & 3);
+                st[i[r]] = a[r];
+            }
+        }
     }
 }
 
@@ -276,57 +337,47 @@ Coef<T> sqrt2_coef()
     return coef<T>(T(std::sqrt(2)), T(0));
 }
 
-// Share of the dense updates' outputs computed on the integer pipes
-// (a mask over the four outputs of a pair, two of a diagonal update).
-// QSLC_EMU_MASK overrides it for tuning sweeps.
-int emu_mask_pair()
+// Share of the dense updates' outputs computed on the integer pipes, as a
+// pattern of one mask per sweep item (see ITEMS): bit i of a pair mask is
+// output i of the pair (r0.x, r0.y, r1.x, r1.y), bit i of a diagonal mask
+// output i of the amplitude.  The defaults balance the FP64 pipe against
+// the integer pipes on GB300; QSLC_EMU_MASK (rotations), QSLC_EMU_MASK_H
+// (Hadamard) and QSLC_EMU_MASK_DIAG (phase) override them for tuning, as
+// "m" (every item) or "m0,m1,m2".
+unsigned parse_pattern(const char *var, const char *dflt, unsigned width_mask)
 {
-    static int m = [] {
-        const char *e = std::getenv("QSLC_EMU_MASK");
-        return e ? std::atoi(e) & 15 : 5;
-    }();
-    return m;
+    const char *e = std::getenv(var);
+    const char *src = e ? e : dflt;
+    unsigned m[ITEMS] = {0, 0, 0};
+    int n = 0;
+    for (const char *c = src; *c && n < ITEMS;) {
+        char *endp = nullptr;
+        const long v = std::strtol(c, &endp, 10);
+        if (endp == c) break;
+        m[n++] = unsigned(v) & width_mask;
+        c = (*endp == ',') ? endp + 1 : endp;
+        if (*endp != ',') break;
+    }
+    for (int i = n; i < ITEMS; i++) m[i] = n ? m[n - 1] : 0;
+    unsigned pat = 0;
+    for (int i = 0; i < ITEMS; i++) pat |= m[i] << (4 * i);
+    return pat;
 }
-int emu_mask_diag()
+unsigned pattern_rot()
 {
-    static int m = [] {
-        const char *e = std::getenv("QSLC_EMU_MASK_DIAG");
-        return e ? std::atoi(e) & 3 : 1;
-    }();
-    return m;
+    static unsigned p = parse_pattern("QSLC_EMU_MASK", "5,5,1", 15);
+    return p;
 }
-
-// launch a kernel template instantiated for the current emulation mask
-#define WITH_PAIR_MASK(T, CALL)                                      \
-    do {                                                             \
-        if constexpr (sizeof(T) == 8) {                              \
-            switch (emu_mask_pair()) {                               \
-            case 1: { constexpr int EMV = 1; CALL; } break;          \
-            case 3: { constexpr int EMV = 3; CALL; } break;          \
-            case 7: { constexpr int EMV = 7; CALL; } break;          \
-            case 15: { constexpr int EMV = 15; CALL; } break;        \
-            case 5: { constexpr int EMV = 5; CALL; } break;          \
-            default: { constexpr int EMV = 0; CALL; } break;         \
-            }                                                        \
-        } else {                                                     \
-            constexpr int EMV = 0;                                   \
-            CALL;                                                    \
-        }                                                            \
-    } while (0)
-#define WITH_DIAG_MASK(T, CALL)                                      \
-    do {                                                             \
-        if constexpr (sizeof(T) == 8) {                              \
-            switch (emu_mask_diag()) {                               \
-            case 1: { constexpr int EMV = 1; CALL; } break;          \
-            case 2: { constexpr int EMV = 2; CALL; } break;          \
-            case 3: { constexpr int EMV = 3; CALL; } break;          \
-            default: { constexpr int EMV = 0; CALL; } break;         \
-            }                                                        \
-        } else {                                                     \
-            constexpr int EMV = 0;                                   \
-            CALL;                                                    \
-        }                                                            \
-    } while (0)
+unsigned pattern_h()
+{
+    static unsigned p = parse_pattern("QSLC_EMU_MASK_H", "0", 15);
+    return p;
+}
+unsigned pattern_diag()
+{
+    static unsigned p = parse_pattern("QSLC_EMU_MASK_DIAG", "1,1,0", 3);
+    return p;
+}
 
 template <class T>
 int gate1_t(qslc_state *s, int gate, unsigned t, double angle)
@@ -335,25 +386,17 @@ int gate1_t(qslc_state *s, int gate, unsigned t, double angle)
     const uint64_t half = uint64_t(1) << (s->n - 1);
     const unsigned grid = grid_for(half);
     cudaStream_t str = s->stream;
+    const bool dp = sizeof(T) == 8;
+    const unsigned rot = dp ? pattern_rot() : 0, had = dp ? pattern_h() : 0, dg = dp ? pattern_diag() : 0;
     switch (gate) {
-    case QSLC_PAULI_X: k_pair1<T, P_SWAP><<<grid, 256, 0, str>>>(st, half, t, Coef<T>{}); break;
-    case QSLC_PAULI_Y: k_pair1<T, P_Y><<<grid, 256, 0, str>>>(st, half, t, Coef<T>{}); break;
-    case QSLC_HADAMARD:
-        WITH_PAIR_MASK(T, (k_pair1<T, P_H, EMV><<<grid, 256, 0, str>>>(st, half, t, sqrt2_coef<T>())));
-        break;
-    case QSLC_ROTATE_X:
-        WITH_PAIR_MASK(T, (k_pair1<T, P_RX, EMV><<<grid, 256, 0, str>>>(st, half, t, half_angle<T>(angle))));
-        break;
-    case QSLC_ROTATE_Y:
-        WITH_PAIR_MASK(T, (k_pair1<T, P_RY, EMV><<<grid, 256, 0, str>>>(st, half, t, half_angle<T>(angle))));
-        break;
-    case QSLC_ROTATE_Z:
-        WITH_PAIR_MASK(T, (k_pair1<T, P_RZ, EMV><<<grid, 256, 0, str>>>(st, half, t, half_angle<T>(angle))));
-        break;
-    case QSLC_PAULI_Z: k_diag1<T, D_NEG><<<grid, 256, 0, str>>>(st, half, t, Coef<T>{}); break;
-    case QSLC_PHASE:
-        WITH_DIAG_MASK(T, (k_diag1<T, D_PHASE, EMV><<<grid, 256, 0, str>>>(st, half, t, full_angle<T>(angle))));
-        break;
+    case QSLC_PAULI_X: k_pair1<T, P_SWAP><<<grid, 256, 0, str>>>(st, half, t, Coef<T>{}, 0); break;
+    case QSLC_PAULI_Y: k_pair1<T, P_Y><<<grid, 256, 0, str>>>(st, half, t, Coef<T>{}, 0); break;
+    case QSLC_HADAMARD: k_pair1<T, P_H><<<grid, 256, 0, str>>>(st, half, t, sqrt2_coef<T>(), had); break;
+    case QSLC_ROTATE_X: k_pair1<T, P_RX><<<grid, 256, 0, str>>>(st, half, t, half_angle<T>(angle), rot); break;
+    case QSLC_ROTATE_Y: k_pair1<T, P_RY><<<grid, 256, 0, str>>>(st, half, t, half_angle<T>(angle), rot); break;
+    case QSLC_ROTATE_Z: k_pair1<T, P_RZ><<<grid, 256, 0, str>>>(st, half, t, half_angle<T>(angle), rot); break;
+    case QSLC_PAULI_Z: k_diag1<T, D_NEG><<<grid, 256, 0, str>>>(st, half, t, Coef<T>{}, 0); break;
+    case QSLC_PHASE: k_diag1<T, D_PHASE><<<grid, 256, 0, str>>>(st, half, t, full_angle<T>(angle), dg); break;
     default: return fail(QSLC_EINVAL, "unknown one-qubit gate code " + std::to_string(gate));
     }
     s->launches++;
@@ -370,32 +413,30 @@ int gate2_t(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle)
     const uint64_t b1 = uint64_t(1) << q1, b2 = uint64_t(1) << q2;
     const unsigned grid = grid_for(quads);
     cudaStream_t str = s->stream;
-#define P2(OP, MODE, K) k_pair2<T, OP, MODE><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1, b2, K)
-#define P2E(OP, MODE, K) \
-    WITH_PAIR_MASK(T, (k_pair2<T, OP, MODE, EMV><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1, b2, K)))
+    const bool dp = sizeof(T) == 8;
+    const unsigned rot = dp ? pattern_rot() : 0, had = dp ? pattern_h() : 0, dg = dp ? pattern_diag() : 0;
+#define P2(OP, MODE, K, PAT) k_pair2<T, OP, MODE><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1, b2, K, PAT)
     switch (gate) {
-    case QSLC_CONTROL_NOT: P2(P_SWAP, 0, Coef<T>{}); break;
-    case QSLC_CONTROL_Y: P2(P_Y, 0, Coef<T>{}); break;
-    case QSLC_CONTROL_ROTATE_X: P2E(P_RX, 0, half_angle<T>(angle)); break;
-    case QSLC_CONTROL_ROTATE_Y: P2E(P_RY, 0, half_angle<T>(angle)); break;
-    case QSLC_CONTROL_ROTATE_Z: P2E(P_RZ, 0, half_angle<T>(angle)); break;
-    case QSLC_CONTROL_HADAMARD: P2E(P_H, 0, sqrt2_coef<T>()); break;
-    case QSLC_SWAP: P2(P_SWAP, 1, Coef<T>{}); break;
-    case QSLC_NP_ROTATE_X: P2E(P_RX, 1, half_angle<T>(angle)); break;
-    case QSLC_NP_ROTATE_Y: P2E(P_RY, 1, half_angle<T>(angle)); break;
-    case QSLC_NP_HADAMARD: P2E(P_H, 1, sqrt2_coef<T>()); break;
-    case QSLC_FSWAP: P2(P_SWAP, 2, Coef<T>{}); break;
+    case QSLC_CONTROL_NOT: P2(P_SWAP, 0, Coef<T>{}, 0); break;
+    case QSLC_CONTROL_Y: P2(P_Y, 0, Coef<T>{}, 0); break;
+    case QSLC_CONTROL_ROTATE_X: P2(P_RX, 0, half_angle<T>(angle), rot); break;
+    case QSLC_CONTROL_ROTATE_Y: P2(P_RY, 0, half_angle<T>(angle), rot); break;
+    case QSLC_CONTROL_ROTATE_Z: P2(P_RZ, 0, half_angle<T>(angle), rot); break;
+    case QSLC_CONTROL_HADAMARD: P2(P_H, 0, sqrt2_coef<T>(), had); break;
+    case QSLC_SWAP: P2(P_SWAP, 1, Coef<T>{}, 0); break;
+    case QSLC_NP_ROTATE_X: P2(P_RX, 1, half_angle<T>(angle), rot); break;
+    case QSLC_NP_ROTATE_Y: P2(P_RY, 1, half_angle<T>(angle), rot); break;
+    case QSLC_NP_HADAMARD: P2(P_H, 1, sqrt2_coef<T>(), had); break;
+    case QSLC_FSWAP: P2(P_SWAP, 2, Coef<T>{}, 0); break;
     case QSLC_CONTROL_Z:
-        k_diag2<T, D_NEG><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1 | b2, Coef<T>{});
+        k_diag2<T, D_NEG><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1 | b2, Coef<T>{}, 0);
         break;
     case QSLC_CONTROL_PHASE:
-        WITH_DIAG_MASK(T, (k_diag2<T, D_PHASE, EMV><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1 | b2,
-                                                                            full_angle<T>(angle))));
+        k_diag2<T, D_PHASE><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1 | b2, full_angle<T>(angle), dg);
         break;
     default: return fail(QSLC_EINVAL, "unknown two-qubit gate code " + std::to_string(gate));
     }
 #undef P2
-#undef P2E
     s->launches++;
     QSLC_CUDA(cudaGetLastError());
     return QSLC_OK;

@@ -30,7 +30,7 @@ static double make(int emin, int emax)
 int main(int argc, char **argv)
 {
     const long N = argc > 1 ? std::atol(argv[1]) : 20000000;
-    long fails = 0, declined_mul = 0, declined_add = 0, declined_dot = 0;
+    long fails = 0, declined_mul = 0, declined_add = 0, declined_dot = 0, declined_div = 0;
     for (long i = 0; i < N; i++) {
         // multiply: constant-like c, amplitude-like a, plus edge exponents
         double c = (i & 7) == 0 ? make(-1022, 1023) : make(-6, 1);
@@ -77,6 +77,34 @@ int main(int argc, char **argv)
             if (ok && qd != dbits(qref)) {
                 if (fails++ < 10) std::printf("div %a / %a: got %a want %a\n", xv, yv, dfrom(qd), (double)qref);
             }
+            // the unpacked division must agree with the packed one bit for bit
+            {
+                bool ok2 = kd.usable != 0;
+                const Unp ux = unpack(dbits(xv), ok2);
+                const uint64_t qu = div_unp(ux, kd, ok2);
+                if (ok2 && qu != dbits(qref)) {
+                    if (fails++ < 10)
+                        std::printf("div_unp %a / %a: got %a want %a\n", xv, yv, dfrom(qu), (double)qref);
+                }
+                if (!ok2) declined_div++;
+            }
+            // a Hadamard output, RN(RN(a +- b) / sqrt2), with the sum unpacked
+            {
+                const double ha = make(-60, 1), hb = (i & 7) == 3 ? ha : make(-62, 1);
+                const bool hneg = rng() & 1;
+                bool ok3 = kd.usable != 0;
+                const Unp sa = unpack(dbits(ha), ok3);
+                Unp sb = unpack(dbits(hb), ok3);
+                if (hneg) sb.sign ^= SIGN;
+                const uint64_t hq = div_unp(add_core(sa, sb, ok3), kd, ok3);
+                volatile double hs = hneg ? ha - hb : ha + hb;
+                volatile double href = hs / yv;
+                if (ok3 && hq != dbits(href)) {
+                    if (fails++ < 10)
+                        std::printf("hdiv (%a %c %a) / %a: got %a want %a\n", ha, hneg ? '-' : '+', hb, yv,
+                                    dfrom(hq), (double)href);
+                }
+            }
             // exact quotients and exact halfway cases: x = q * y for short q
             double qv = make(-4, 4);
             double prod = qv * yv;
@@ -85,6 +113,12 @@ int main(int argc, char **argv)
             volatile double qref2 = prod / yv;
             if (ok && qd != dbits(qref2)) {
                 if (fails++ < 10) std::printf("div2 %a / %a: got %a want %a\n", prod, yv, dfrom(qd), (double)qref2);
+            }
+            bool ok4 = kd.usable != 0;
+            const uint64_t qu2 = div_unp(unpack(dbits(prod), ok4), kd, ok4);
+            if (ok4 && qu2 != dbits(qref2)) {
+                if (fails++ < 10)
+                    std::printf("div_unp2 %a / %a: got %a want %a\n", prod, yv, dfrom(qu2), (double)qref2);
             }
         }
         // the fused shape of a rotation output, RN(RN(a*c) +- RN(b*s)), with
@@ -118,7 +152,7 @@ int main(int argc, char **argv)
                 declined_add, declined_dot);
     if (fails) return 1;
     // declines must be rare on amplitude-like data
-    if (declined_add > N / 100 || declined_dot > N / 50) return 2;
+    if (declined_add > N / 100 || declined_dot > N / 50 || declined_div > N / 50) return 2;
     std::puts("dpemu ok");
     return 0;
 }

@@ -1,10 +1,11 @@
 """Every split of the dense gate arithmetic between the FP64 pipe and the
 integer-pipe binary64 emulation gives the oracle's bits.
 
-QSLC_EMU_MASK selects which of the four outputs of an amplitude pair (and
-QSLC_EMU_MASK_DIAG which of the two outputs of a diagonal update) the
-integer pipes compute; the library reads them once per process, so each
-setting runs in its own process."""
+QSLC_EMU_MASK (rotations) and QSLC_EMU_MASK_H (Hadamard) select which of
+the four outputs of an amplitude pair, and QSLC_EMU_MASK_DIAG which of the
+two outputs of a diagonal update, the integer pipes compute -- one mask per
+item of a sweep iteration ("m" or "m0,m1,m2").  The library reads them
+once per process, so each setting runs in its own process."""
 import os
 import subprocess
 import sys
@@ -46,15 +47,17 @@ def circuit(rng, n, reps):
     return np.array(names), np.array(q1), np.array(q2), np.array(ang)
 
 
-@pytest.mark.parametrize("pair,diag", [(0, 0), (1, 2), (3, 1), (5, 3), (7, 1), (15, 3)])
-def test_every_emulation_split_is_exact(qsl, port, tmp_path, pair, diag):
-    rng = np.random.default_rng(pair * 7 + diag)
+@pytest.mark.parametrize("rot,had,diag", [("0", "0", "0"), ("1", "5", "2"), ("3,5,1", "15", "1,0,3"),
+                                          ("5,5,1", "0", "1,1,0"), ("7", "3,1,0", "3"),
+                                          ("15", "15", "3"), ("10,12,6", "9", "2,1")])
+def test_every_emulation_split_is_exact(qsl, port, tmp_path, rot, had, diag):
+    rng = np.random.default_rng(len(rot) * 7 + len(diag) + int(had.split(",")[0]))
     n = 12
     st = random_state(rng, n)
     names, q1, q2, ang = circuit(rng, n, 6)
     inp, out = str(tmp_path / "in.npz"), str(tmp_path / "out.npy")
     np.savez(inp, state=st, names=names, q1=q1, q2=q2, ang=ang)
-    env = dict(os.environ, QSLC_EMU_MASK=str(pair), QSLC_EMU_MASK_DIAG=str(diag))
+    env = dict(os.environ, QSLC_EMU_MASK=rot, QSLC_EMU_MASK_H=had, QSLC_EMU_MASK_DIAG=diag)
     r = subprocess.run([sys.executable, "-c", SCRIPT.format(root=ROOT, inp=inp, out=out)],
                        env=env, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
