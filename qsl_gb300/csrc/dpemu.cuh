@@ -400,15 +400,12 @@ QSLC_HD uint64_t div_unp(const Unp &x, const DivConst &y, bool &ok)
     const uint64_t k53 = uint64_t(mx < y.m);
     uint64_t t = (hi << k53) | ((mid >> 31) & k53);  // bit 63 of the truncated product is bit 31 of mid
     uint64_t r = (mx << (52 + k53)) - t * y.m;
-    const uint64_t c1 = uint64_t(r >= y.m);
-    t += c1;
-    r -= c1 * y.m;
-    const uint64_t c2 = uint64_t(r >= y.m);
-    t += c2;
-    r -= c2 * y.m;
-    const uint64_t c3 = uint64_t(r >= y.m);
-    t += c3;
-    r -= c3 * y.m;
+#pragma unroll
+    for (int step = 0; step < 3; step++) {
+        const bool c = r >= y.m;
+        t += c ? 1 : 0;
+        r -= c ? y.m : 0;
+    }
     const uint64_t r2 = r << 1;
     t += uint64_t(r2 > y.m) | (uint64_t(r2 == y.m) & (t & 1));
     int e = x.e - y.e - int(k53);

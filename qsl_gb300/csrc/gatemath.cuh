@@ -1,0 +1,194 @@
+// gatemath.cuh -- the arithmetic of one gate output, shared by the plain
+// sweeps (gates.cu) and the number-preserving sweeps (np.cu).
+//
+// Every output is computed as the reference computes it, operation for
+// operation, with each product and sum rounded on its own (no FMA).  For
+// complex128 an output can instead run on the integer pipes through the
+// exact binary64 emulation of dpemu.cuh; the bits are the same either way,
+// and the split between the FP64 pipe and the integer pipes is chosen per
+// sweep item by a pattern of masks.
+#pragma once
+
+#include "qslc_internal.cuh"
+#include "dpemu.cuh"
+
+#include <cmath>
+#include <cstdlib>
+#include <type_traits>
+
+namespace qslc {
+
+template <class T>
+struct Coef {
+    T c, s;  // cos/sin of angle/2 (rotations) or of angle (phase); sqrt2 for H
+    emu::MulConst kc, ks;   // c and s decoded for the integer path (double only)
+    emu::DivConst kd;       // c as a divisor (Hadamard)
+};
+
+// One Hadamard output, RN(RN(a +- b) / sqrt2) (gates.cpp:95-98).  The
+// division always runs on the integer pipes (an FP64 divide is a long
+// iteration on the FP64 pipe); with `em` set the sum does too.
+template <class T, bool NEG>
+__device__ __forceinline__ T hdiv(bool em, T a, T b, const Coef<T> &k)
+{
+    using R = rn<T>;
+    if constexpr (sizeof(T) == 8) {
+        bool ok = k.kd.usable != 0;
+        if (ok) {
+            emu::Unp sum;
+            if (em) {
+                const emu::Unp x = emu::unpack(emu::dbits(a), ok);
+                emu::Unp y = emu::unpack(emu::dbits(b), ok);
+                if (NEG) y.sign ^= emu::SIGN;
+                sum = emu::add_core(x, y, ok);
+            } else {
+                sum = emu::unpack(emu::dbits(NEG ? R::sub(a, b) : R::add(a, b)), ok);
+            }
+            const uint64_t q = emu::div_unp(sum, k.kd, ok);
+            if (ok) return emu::dfrom(q);
+        }
+    }
+    return R::div(NEG ? R::sub(a, b) : R::add(a, b), k.c);
+}
+
+// One output of a rotation or phase update: RN(RN(a*k1) + RN(b*k2)), or
+// RN(RN(a*k1) - RN(b*k2)) when NEG.  With `em` set the integer pipes compute it
+// (dpemu.cuh), falling back to the FP64 pipe for operands the integer path
+// declines; either way the bits are the reference's.
+template <class T, bool NEG>
+__device__ __forceinline__ T dot2(bool em, T a, T k1, const emu::MulConst &e1, T b, T k2,
+                                  const emu::MulConst &e2)
+{
+    if constexpr (sizeof(T) == 8) {
+        bool ok = em && (e1.usable & e2.usable) != 0;
+        if (ok) {
+            const uint64_t r = emu::dot2_rn(emu::dbits(a), e1, emu::dbits(b), e2, NEG, ok);
+            if (ok) return emu::dfrom(r);
+        }
+    }
+    using R = rn<T>;
+    return NEG ? R::sub(R::mul(a, k1), R::mul(b, k2)) : R::add(R::mul(a, k1), R::mul(b, k2));
+}
+
+// The sweeps below take ITEMS work items per grid-stride iteration (at j,
+// j + stride, j + 2 stride), all loads first.  `pat` holds one emulation
+// mask per item, 4 bits each: item r uses (pat >> 4r) & 15, so the share of
+// outputs computed on the integer pipes can be set in steps of one output
+// in twelve (pair gates) or one in six (diagonal gates).  Masks differ only
+// between items, never between threads of a warp.
+constexpr int ITEMS = 3;
+
+// A kernel's pattern is a template argument when it is one of the few
+// compiled in (the mask tests then fold away, and so do the unused
+// arithmetic paths and their registers); PAT_RUNTIME takes it from the
+// kernel's argument instead, for any other setting.
+constexpr unsigned PAT_RUNTIME = 0xFFFFFFFFu;
+
+// The patterns compiled in: the defaults below and their neighbours, so a
+// tuning sweep near the default measures compiled code too.
+#define QSLC_ROT_PATTERNS 0u, 0x115u, 0x155u, 0x111u, 0x555u, 0x151u
+#define QSLC_H_PATTERNS 0u, 0x001u, 0x011u
+#define QSLC_DIAG_PATTERNS 0u, 0x011u, 0x001u, 0x111u
+#define QSLC_NP_PAIR_PATTERNS 0u, 0x115u, 0x111u, 0x011u, 0x001u
+#define QSLC_NP_DIAG_PATTERNS 0u, 0x001u, 0x011u
+
+// Launch `f(std::integral_constant<unsigned, P>{})` with P = pat when pat is
+// one of CANDIDATES, else with PAT_RUNTIME.
+template <unsigned... CANDIDATES, class F>
+void with_pattern(unsigned pat, F &&f)
+{
+    bool done = false;
+    ((pat == CANDIDATES && !done ? (f(std::integral_constant<unsigned, CANDIDATES>{}), done = true) : false),
+     ...);
+    if (!done) f(std::integral_constant<unsigned, PAT_RUNTIME>{});
+}
+
+// Host-side coefficients, computed exactly as the reference does: in Fp,
+// with std::cos/std::sin of angle/2 (gates.cpp:124-125) or of angle
+// (:106), and sqrt2 = Fp(std::sqrt(2)) (:94).
+template <class T>
+Coef<T> coef(T c, T s)
+{
+    Coef<T> k{};
+    k.c = c;
+    k.s = s;
+    k.kc = emu::make_const(double(c));
+    k.ks = emu::make_const(double(s));
+    k.kd = emu::make_div(double(c));
+    return k;
+}
+template <class T>
+Coef<T> half_angle(double angle)
+{
+    T a = T(angle);
+    return coef<T>(T(std::cos(a / 2)), T(std::sin(a / 2)));
+}
+template <class T>
+Coef<T> full_angle(double angle)
+{
+    T a = T(angle);
+    return coef<T>(T(std::cos(a)), T(std::sin(a)));
+}
+template <class T>
+Coef<T> sqrt2_coef()
+{
+    return coef<T>(T(std::sqrt(2)), T(0));
+}
+
+// Share of the dense updates' outputs computed on the integer pipes, as a
+// pattern of one mask per sweep item (see ITEMS): bit i of a pair mask is
+// output i of the pair (r0.x, r0.y, r1.x, r1.y), bit i of a diagonal mask
+// output i of the amplitude.  The defaults balance the FP64 pipe against
+// the integer pipes on GB300; QSLC_EMU_MASK (rotations), QSLC_EMU_MASK_H
+// (Hadamard) and QSLC_EMU_MASK_DIAG (phase) override them for tuning, as
+// "m" (every item) or "m0,m1,m2".
+inline unsigned parse_pattern(const char *var, const char *dflt, unsigned width_mask)
+{
+    const char *e = std::getenv(var);
+    const char *src = e ? e : dflt;
+    unsigned m[ITEMS] = {0, 0, 0};
+    int n = 0;
+    for (const char *c = src; *c && n < ITEMS;) {
+        char *endp = nullptr;
+        const long v = std::strtol(c, &endp, 10);
+        if (endp == c) break;
+        m[n++] = unsigned(v) & width_mask;
+        c = (*endp == ',') ? endp + 1 : endp;
+        if (*endp != ',') break;
+    }
+    for (int i = n; i < ITEMS; i++) m[i] = n ? m[n - 1] : 0;
+    unsigned pat = 0;
+    for (int i = 0; i < ITEMS; i++) pat |= m[i] << (4 * i);
+    return pat;
+}
+inline unsigned pattern_rot()
+{
+    static unsigned p = parse_pattern("QSLC_EMU_MASK", "5,1,1", 15);
+    return p;
+}
+inline unsigned pattern_h()
+{
+    static unsigned p = parse_pattern("QSLC_EMU_MASK_H", "0", 15);
+    return p;
+}
+inline unsigned pattern_diag()
+{
+    static unsigned p = parse_pattern("QSLC_EMU_MASK_DIAG", "1,1,0", 3);
+    return p;
+}
+// The number-preserving sweeps spend integer work on ranking their indices,
+// so they keep a smaller share of the arithmetic on the integer pipes:
+// QSLC_EMU_MASK_NP (pair gates) and QSLC_EMU_MASK_NP_DIAG (single
+// amplitudes).
+inline unsigned pattern_np_pair()
+{
+    static unsigned p = parse_pattern("QSLC_EMU_MASK_NP", "5,1,1", 15);
+    return p;
+}
+inline unsigned pattern_np_diag()
+{
+    static unsigned p = parse_pattern("QSLC_EMU_MASK_NP_DIAG", "1,0,0", 3);
+    return p;
+}
+
+}  // namespace qslc

@@ -12,7 +12,7 @@
 // contraction into FMA: the x86-64 reference rounds each product and each
 // sum, and so does every update below (rn<T>::mul/add/sub/div).
 #include "qslc_internal.cuh"
-#include "dpemu.cuh"
+#include "gatemath.cuh"
 
 #include <cmath>
 #include <cstdlib>
@@ -22,58 +22,6 @@ namespace {
 
 enum PairOp { P_SWAP, P_Y, P_H, P_RX, P_RY, P_RZ };
 enum DiagOp { D_NEG, D_PHASE };
-
-template <class T>
-struct Coef {
-    T c, s;  // cos/sin of angle/2 (rotations) or of angle (phase); sqrt2 for H
-    emu::MulConst kc, ks;   // c and s decoded for the integer path (double only)
-    emu::DivConst kd;       // c as a divisor (Hadamard)
-};
-
-// One Hadamard output, RN(RN(a +- b) / sqrt2) (gates.cpp:95-98).  The
-// division always runs on the integer pipes (an FP64 divide is a long
-// iteration on the FP64 pipe); with EMU the sum does too.
-template <class T, bool NEG>
-__device__ __forceinline__ T hdiv(bool em, T a, T b, const Coef<T> &k)
-{
-    using R = rn<T>;
-    if constexpr (sizeof(T) == 8) {
-        bool ok = k.kd.usable != 0;
-        if (ok) {
-            emu::Unp sum;
-            if (em) {
-                const emu::Unp x = emu::unpack(emu::dbits(a), ok);
-                emu::Unp y = emu::unpack(emu::dbits(b), ok);
-                if (NEG) y.sign ^= emu::SIGN;
-                sum = emu::add_core(x, y, ok);
-            } else {
-                sum = emu::unpack(emu::dbits(NEG ? R::sub(a, b) : R::add(a, b)), ok);
-            }
-            const uint64_t q = emu::div_unp(sum, k.kd, ok);
-            if (ok) return emu::dfrom(q);
-        }
-    }
-    return R::div(NEG ? R::sub(a, b) : R::add(a, b), k.c);
-}
-
-// One output of a rotation or phase update: RN(RN(a*k1) + RN(b*k2)), or
-// RN(RN(a*k1) - RN(b*k2)) when NEG.  With EMU the integer pipes compute it
-// (dpemu.cuh), falling back to the FP64 pipe for operands the integer path
-// declines; either way the bits are the reference's.
-template <class T, bool NEG>
-__device__ __forceinline__ T dot2(bool em, T a, T k1, const emu::MulConst &e1, T b, T k2,
-                                  const emu::MulConst &e2)
-{
-    if constexpr (sizeof(T) == 8) {
-        bool ok = em && (e1.usable & e2.usable) != 0;
-        if (ok) {
-            const uint64_t r = emu::dot2_rn(emu::dbits(a), e1, emu::dbits(b), e2, NEG, ok);
-            if (ok) return emu::dfrom(r);
-        }
-    }
-    using R = rn<T>;
-    return NEG ? R::sub(R::mul(a, k1), R::mul(b, k2)) : R::add(R::mul(a, k1), R::mul(b, k2));
-}
 
 // em: bit i set = output i (r0.x, r0.y, r1.x, r1.y) on the integer pipes;
 // it must be the same across a warp.
@@ -128,21 +76,14 @@ __device__ __forceinline__ void diag_update(cplx<T> &a, const Coef<T> &k, unsign
     }
 }
 
-// The sweeps below take ITEMS work items per grid-stride iteration (at j,
-// j + stride, j + 2 stride), all loads first.  `pat` holds one emulation
-// mask per item, 4 bits each: item r uses (pat >> 4r) & 15, so the share of
-// outputs computed on the integer pipes can be set in steps of one output
-// in twelve (pair gates) or one in six (diagonal gates).  Masks differ only
-// between items, never between threads of a warp.
-constexpr int ITEMS = 3;
-
 // One-qubit pair gates: pairs (i0, i0 + 2^t), i0 = insert0(j, t).
-template <class T, int OP>
+template <class T, int OP, unsigned CPAT = PAT_RUNTIME>
 __global__ void __launch_bounds__(256) k_pair1(cplx<T> *__restrict__ st, uint64_t npairs,
                                                unsigned t, Coef<T> k, unsigned pat)
 {
     const uint64_t bit = uint64_t(1) << t;
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    const unsigned pt = CPAT == PAT_RUNTIME ? pat : CPAT;
     for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < npairs; j += ITEMS * stride) {
         cplx<T> a0[ITEMS], a1[ITEMS];
         uint64_t i0[ITEMS];
@@ -157,7 +98,7 @@ __global__ void __launch_bounds__(256) k_pair1(cplx<T> *__restrict__ st, uint64_
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
             if (j + r * stride < npairs) {
-                pair_update<T, OP>(a0[r], a1[r], k, (pat >> (4 * r)) & 15);
+                pair_update<T, OP>(a0[r], a1[r], k, (pt >> (4 * r)) & 15);
                 st[i0[r]] = a0[r];
                 st[i0[r] | bit] = a1[r];
             }
@@ -166,12 +107,13 @@ __global__ void __launch_bounds__(256) k_pair1(cplx<T> *__restrict__ st, uint64_
 }
 
 // One-qubit diagonal gates on the |1> half: index insert0(j, t) | 2^t.
-template <class T, int OP>
+template <class T, int OP, unsigned CPAT = PAT_RUNTIME>
 __global__ void __launch_bounds__(256) k_diag1(cplx<T> *__restrict__ st, uint64_t count,
                                                unsigned t, Coef<T> k, unsigned pat)
 {
     const uint64_t bit = uint64_t(1) << t;
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    const unsigned pt = CPAT == PAT_RUNTIME ? pat : CPAT;
     for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < count; j += ITEMS * stride) {
         cplx<T> a[ITEMS];
         uint64_t i[ITEMS];
@@ -183,7 +125,7 @@ __global__ void __launch_bounds__(256) k_diag1(cplx<T> *__restrict__ st, uint64_
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
             if (j + r * stride < count) {
-                diag_update<T, OP>(a[r], k, (pat >> (4 * r)) & 3);
+                diag_update<T, OP>(a[r], k, (pt >> (4 * r)) & 3);
                 st[i[r]] = a[r];
             }
         }
@@ -197,12 +139,13 @@ __global__ void __launch_bounds__(256) k_diag1(cplx<T> *__restrict__ st, uint64_
 // MODE 0: controlled pair (base|b1, base|b1|b2), b1 = control bit;
 // MODE 1: number-preserving pair (base|b1, base|b2);
 // MODE 2: fswap = MODE 1 swap plus negation of base|b1|b2.
-template <class T, int OP, int MODE>
+template <class T, int OP, int MODE, unsigned CPAT = PAT_RUNTIME>
 __global__ void __launch_bounds__(256) k_pair2(cplx<T> *__restrict__ st, uint64_t nquads,
                                                unsigned lo, unsigned hi, uint64_t b1,
                                                uint64_t b2, Coef<T> k, unsigned pat)
 {
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    const unsigned pt = CPAT == PAT_RUNTIME ? pat : CPAT;
     for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < nquads; j += ITEMS * stride) {
         cplx<T> a0[ITEMS], a1[ITEMS];
         uint64_t x1[ITEMS], x2[ITEMS];
@@ -219,7 +162,7 @@ __global__ void __launch_bounds__(256) k_pair2(cplx<T> *__restrict__ st, uint64_
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
             if (j + r * stride < nquads) {
-                pair_update<T, OP>(a0[r], a1[r], k, (pat >> (4 * r)) & 15);
+                pair_update<T, OP>(a0[r], a1[r], k, (pt >> (4 * r)) & 15);
                 st[x1[r]] = a0[r];
                 st[x2[r]] = a1[r];
                 if constexpr (MODE == 2) {
@@ -234,12 +177,13 @@ __global__ void __launch_bounds__(256) k_pair2(cplx<T> *__restrict__ st, uint64_
 }
 
 // controlZ / controlPhase: the |11> quarter (gates.cpp:277-301, :436-465).
-template <class T, int OP>
+template <class T, int OP, unsigned CPAT = PAT_RUNTIME>
 __global__ void __launch_bounds__(256) k_diag2(cplx<T> *__restrict__ st, uint64_t nquads,
                                                unsigned lo, unsigned hi, uint64_t both,
                                                Coef<T> k, unsigned pat)
 {
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    const unsigned pt = CPAT == PAT_RUNTIME ? pat : CPAT;
     for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < nquads; j += ITEMS * stride) {
         cplx<T> a[ITEMS];
         uint64_t i[ITEMS];
@@ -251,7 +195,7 @@ __global__ void __launch_bounds__(256) k_diag2(cplx<T> *__restrict__ st, uint64_
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
             if (j + r * stride < nquads) {
-                diag_update<T, OP>(a[r], k, (pat >> (4 * r)) & 3);
+                diag_update<T, OP>(a[r], k, (pt >> (4 * r)) & 3);
                 st[i[r]] = a[r];
             }
         }
@@ -305,80 +249,6 @@ __global__ void k_set_one(cplx<T> *st, uint64_t pos)
     st[pos] = one;
 }
 
-// Host-side coefficients, computed exactly as the reference does: in Fp,
-// with std::cos/std::sin of angle/2 (gates.cpp:124-125) or of angle
-// (:106), and sqrt2 = Fp(std::sqrt(2)) (:94).
-template <class T>
-Coef<T> coef(T c, T s)
-{
-    Coef<T> k{};
-    k.c = c;
-    k.s = s;
-    k.kc = emu::make_const(double(c));
-    k.ks = emu::make_const(double(s));
-    k.kd = emu::make_div(double(c));
-    return k;
-}
-template <class T>
-Coef<T> half_angle(double angle)
-{
-    T a = T(angle);
-    return coef<T>(T(std::cos(a / 2)), T(std::sin(a / 2)));
-}
-template <class T>
-Coef<T> full_angle(double angle)
-{
-    T a = T(angle);
-    return coef<T>(T(std::cos(a)), T(std::sin(a)));
-}
-template <class T>
-Coef<T> sqrt2_coef()
-{
-    return coef<T>(T(std::sqrt(2)), T(0));
-}
-
-// Share of the dense updates' outputs computed on the integer pipes, as a
-// pattern of one mask per sweep item (see ITEMS): bit i of a pair mask is
-// output i of the pair (r0.x, r0.y, r1.x, r1.y), bit i of a diagonal mask
-// output i of the amplitude.  The defaults balance the FP64 pipe against
-// the integer pipes on GB300; QSLC_EMU_MASK (rotations), QSLC_EMU_MASK_H
-// (Hadamard) and QSLC_EMU_MASK_DIAG (phase) override them for tuning, as
-// "m" (every item) or "m0,m1,m2".
-unsigned parse_pattern(const char *var, const char *dflt, unsigned width_mask)
-{
-    const char *e = std::getenv(var);
-    const char *src = e ? e : dflt;
-    unsigned m[ITEMS] = {0, 0, 0};
-    int n = 0;
-    for (const char *c = src; *c && n < ITEMS;) {
-        char *endp = nullptr;
-        const long v = std::strtol(c, &endp, 10);
-        if (endp == c) break;
-        m[n++] = unsigned(v) & width_mask;
-        c = (*endp == ',') ? endp + 1 : endp;
-        if (*endp != ',') break;
-    }
-    for (int i = n; i < ITEMS; i++) m[i] = n ? m[n - 1] : 0;
-    unsigned pat = 0;
-    for (int i = 0; i < ITEMS; i++) pat |= m[i] << (4 * i);
-    return pat;
-}
-unsigned pattern_rot()
-{
-    static unsigned p = parse_pattern("QSLC_EMU_MASK", "5,5,1", 15);
-    return p;
-}
-unsigned pattern_h()
-{
-    static unsigned p = parse_pattern("QSLC_EMU_MASK_H", "0", 15);
-    return p;
-}
-unsigned pattern_diag()
-{
-    static unsigned p = parse_pattern("QSLC_EMU_MASK_DIAG", "1,1,0", 3);
-    return p;
-}
-
 template <class T>
 int gate1_t(qslc_state *s, int gate, unsigned t, double angle)
 {
@@ -388,15 +258,30 @@ int gate1_t(qslc_state *s, int gate, unsigned t, double angle)
     cudaStream_t str = s->stream;
     const bool dp = sizeof(T) == 8;
     const unsigned rot = dp ? pattern_rot() : 0, had = dp ? pattern_h() : 0, dg = dp ? pattern_diag() : 0;
+    auto pair = [&](auto op, unsigned pat, const Coef<T> &k, auto cands) {
+        constexpr int OP = decltype(op)::value;
+        cands(pat, [&](auto c) {
+            k_pair1<T, OP, decltype(c)::value><<<grid, 256, 0, str>>>(st, half, t, k, pat);
+        });
+    };
+    auto rot_c = [](unsigned p, auto f) { with_pattern<QSLC_ROT_PATTERNS>(p, f); };
+    auto h_c = [](unsigned p, auto f) { with_pattern<QSLC_H_PATTERNS>(p, f); };
+    auto none = [](unsigned p, auto f) { with_pattern<0u>(p, f); };
     switch (gate) {
-    case QSLC_PAULI_X: k_pair1<T, P_SWAP><<<grid, 256, 0, str>>>(st, half, t, Coef<T>{}, 0); break;
-    case QSLC_PAULI_Y: k_pair1<T, P_Y><<<grid, 256, 0, str>>>(st, half, t, Coef<T>{}, 0); break;
-    case QSLC_HADAMARD: k_pair1<T, P_H><<<grid, 256, 0, str>>>(st, half, t, sqrt2_coef<T>(), had); break;
-    case QSLC_ROTATE_X: k_pair1<T, P_RX><<<grid, 256, 0, str>>>(st, half, t, half_angle<T>(angle), rot); break;
-    case QSLC_ROTATE_Y: k_pair1<T, P_RY><<<grid, 256, 0, str>>>(st, half, t, half_angle<T>(angle), rot); break;
-    case QSLC_ROTATE_Z: k_pair1<T, P_RZ><<<grid, 256, 0, str>>>(st, half, t, half_angle<T>(angle), rot); break;
-    case QSLC_PAULI_Z: k_diag1<T, D_NEG><<<grid, 256, 0, str>>>(st, half, t, Coef<T>{}, 0); break;
-    case QSLC_PHASE: k_diag1<T, D_PHASE><<<grid, 256, 0, str>>>(st, half, t, full_angle<T>(angle), dg); break;
+    case QSLC_PAULI_X: pair(std::integral_constant<int, P_SWAP>{}, 0, Coef<T>{}, none); break;
+    case QSLC_PAULI_Y: pair(std::integral_constant<int, P_Y>{}, 0, Coef<T>{}, none); break;
+    case QSLC_HADAMARD: pair(std::integral_constant<int, P_H>{}, had, sqrt2_coef<T>(), h_c); break;
+    case QSLC_ROTATE_X: pair(std::integral_constant<int, P_RX>{}, rot, half_angle<T>(angle), rot_c); break;
+    case QSLC_ROTATE_Y: pair(std::integral_constant<int, P_RY>{}, rot, half_angle<T>(angle), rot_c); break;
+    case QSLC_ROTATE_Z: pair(std::integral_constant<int, P_RZ>{}, rot, half_angle<T>(angle), rot_c); break;
+    case QSLC_PAULI_Z: k_diag1<T, D_NEG, 0u><<<grid, 256, 0, str>>>(st, half, t, Coef<T>{}, 0); break;
+    case QSLC_PHASE: {
+        const Coef<T> k = full_angle<T>(angle);
+        with_pattern<QSLC_DIAG_PATTERNS>(dg, [&](auto c) {
+            k_diag1<T, D_PHASE, decltype(c)::value><<<grid, 256, 0, str>>>(st, half, t, k, dg);
+        });
+        break;
+    }
     default: return fail(QSLC_EINVAL, "unknown one-qubit gate code " + std::to_string(gate));
     }
     s->launches++;
@@ -415,28 +300,53 @@ int gate2_t(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle)
     cudaStream_t str = s->stream;
     const bool dp = sizeof(T) == 8;
     const unsigned rot = dp ? pattern_rot() : 0, had = dp ? pattern_h() : 0, dg = dp ? pattern_diag() : 0;
-#define P2(OP, MODE, K, PAT) k_pair2<T, OP, MODE><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1, b2, K, PAT)
+    // pair kernel with operation OP, mode MODE, pattern pat among candidates
+    auto pair = [&](auto op, auto mode, unsigned pat, const Coef<T> &k, auto cands) {
+        constexpr int OP = decltype(op)::value, MODE = decltype(mode)::value;
+        cands(pat, [&](auto c) {
+            k_pair2<T, OP, MODE, decltype(c)::value><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1, b2, k, pat);
+        });
+    };
+    auto rot_c = [](unsigned p, auto f) { with_pattern<QSLC_ROT_PATTERNS>(p, f); };
+    auto h_c = [](unsigned p, auto f) { with_pattern<QSLC_H_PATTERNS>(p, f); };
+    auto none = [](unsigned p, auto f) { with_pattern<0u>(p, f); };
+    using M0 = std::integral_constant<int, 0>;
+    using M1 = std::integral_constant<int, 1>;
+    using M2 = std::integral_constant<int, 2>;
     switch (gate) {
-    case QSLC_CONTROL_NOT: P2(P_SWAP, 0, Coef<T>{}, 0); break;
-    case QSLC_CONTROL_Y: P2(P_Y, 0, Coef<T>{}, 0); break;
-    case QSLC_CONTROL_ROTATE_X: P2(P_RX, 0, half_angle<T>(angle), rot); break;
-    case QSLC_CONTROL_ROTATE_Y: P2(P_RY, 0, half_angle<T>(angle), rot); break;
-    case QSLC_CONTROL_ROTATE_Z: P2(P_RZ, 0, half_angle<T>(angle), rot); break;
-    case QSLC_CONTROL_HADAMARD: P2(P_H, 0, sqrt2_coef<T>(), had); break;
-    case QSLC_SWAP: P2(P_SWAP, 1, Coef<T>{}, 0); break;
-    case QSLC_NP_ROTATE_X: P2(P_RX, 1, half_angle<T>(angle), rot); break;
-    case QSLC_NP_ROTATE_Y: P2(P_RY, 1, half_angle<T>(angle), rot); break;
-    case QSLC_NP_HADAMARD: P2(P_H, 1, sqrt2_coef<T>(), had); break;
-    case QSLC_FSWAP: P2(P_SWAP, 2, Coef<T>{}, 0); break;
+    case QSLC_CONTROL_NOT: pair(std::integral_constant<int, P_SWAP>{}, M0{}, 0, Coef<T>{}, none); break;
+    case QSLC_CONTROL_Y: pair(std::integral_constant<int, P_Y>{}, M0{}, 0, Coef<T>{}, none); break;
+    case QSLC_CONTROL_ROTATE_X:
+        pair(std::integral_constant<int, P_RX>{}, M0{}, rot, half_angle<T>(angle), rot_c);
+        break;
+    case QSLC_CONTROL_ROTATE_Y:
+        pair(std::integral_constant<int, P_RY>{}, M0{}, rot, half_angle<T>(angle), rot_c);
+        break;
+    case QSLC_CONTROL_ROTATE_Z:
+        pair(std::integral_constant<int, P_RZ>{}, M0{}, rot, half_angle<T>(angle), rot_c);
+        break;
+    case QSLC_CONTROL_HADAMARD: pair(std::integral_constant<int, P_H>{}, M0{}, had, sqrt2_coef<T>(), h_c); break;
+    case QSLC_SWAP: pair(std::integral_constant<int, P_SWAP>{}, M1{}, 0, Coef<T>{}, none); break;
+    case QSLC_NP_ROTATE_X:
+        pair(std::integral_constant<int, P_RX>{}, M1{}, rot, half_angle<T>(angle), rot_c);
+        break;
+    case QSLC_NP_ROTATE_Y:
+        pair(std::integral_constant<int, P_RY>{}, M1{}, rot, half_angle<T>(angle), rot_c);
+        break;
+    case QSLC_NP_HADAMARD: pair(std::integral_constant<int, P_H>{}, M1{}, had, sqrt2_coef<T>(), h_c); break;
+    case QSLC_FSWAP: pair(std::integral_constant<int, P_SWAP>{}, M2{}, 0, Coef<T>{}, none); break;
     case QSLC_CONTROL_Z:
-        k_diag2<T, D_NEG><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1 | b2, Coef<T>{}, 0);
+        k_diag2<T, D_NEG, 0u><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1 | b2, Coef<T>{}, 0);
         break;
-    case QSLC_CONTROL_PHASE:
-        k_diag2<T, D_PHASE><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1 | b2, full_angle<T>(angle), dg);
+    case QSLC_CONTROL_PHASE: {
+        const Coef<T> k = full_angle<T>(angle);
+        with_pattern<QSLC_DIAG_PATTERNS>(dg, [&](auto c) {
+            k_diag2<T, D_PHASE, decltype(c)::value><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1 | b2, k, dg);
+        });
         break;
+    }
     default: return fail(QSLC_EINVAL, "unknown two-qubit gate code " + std::to_string(gate));
     }
-#undef P2
     s->launches++;
     QSLC_CUDA(cudaGetLastError());
     return QSLC_OK;

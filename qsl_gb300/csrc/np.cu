@@ -16,6 +16,7 @@
 // as the reference does (np/gates.cpp:39-51, :127-147) and ranks the
 // resulting basis indices to find their slots.  The {n, w} table doubles as
 // the slot -> basis index map used by measurement.
+#include "gatemath.cuh"
 #include "seqsum.cuh"
 #include "np_host.hpp"
 
@@ -105,80 +106,110 @@ enum NPKind {
     NP_SWAP, NP_RX, NP_RY, NP_H                 // two-qubit pairs
 };
 
-template <class T>
-struct NPCoef {
-    T c, s;
-};
-
 // Single-amplitude updates (np/gates.cpp:53-55, :77-78, :104-106, :148-149,
-// :183-185, :229-231).
-template <class T, int K>
+// :183-185, :229-231).  Three items per grid-stride iteration, as in the
+// plain sweeps; `pat` chooses per item which of the two outputs run on the
+// integer pipes (gatemath.cuh).
+template <class T, int K, unsigned CPAT = PAT_RUNTIME>
 __global__ void __launch_bounds__(256) k_np_single(cplx<T> *__restrict__ st,
                                                    const uint32_t *__restrict__ tab, uint64_t count,
                                                    const uint32_t *__restrict__ rt, unsigned t1,
-                                                   unsigned t2, uint32_t addbits, NPCoef<T> k)
+                                                   unsigned t2, uint32_t addbits, Coef<T> k,
+                                                   unsigned pat)
 {
     using R = rn<T>;
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
-    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < count; j += stride) {
-        const uint32_t x = tab[j];
-        uint32_t y;
-        if constexpr (K == NP_PHASE1 || K == NP_NEG1 || K == NP_RZ0)
-            y = ins_bit(x, t1, 0) | addbits;
-        else
-            y = ins00(x, t1, t2) | addbits;
-        const uint32_t slot = rank_dev(rt, y);
-        cplx<T> a = st[slot];
-        if constexpr (K == NP_NEG1 || K == NP_CZ) {
-            a.x = R::mul(a.x, T(-1));
-            a.y = R::mul(a.y, T(-1));
-        } else if constexpr (K == NP_RZ0 || K == NP_CRZ01) {
-            T re = a.x, im = a.y;      // cos*re + sin*im, cos*im - sin*re
-            a.x = R::add(R::mul(k.c, re), R::mul(k.s, im));
-            a.y = R::sub(R::mul(k.c, im), R::mul(k.s, re));
-        } else {
-            T re = a.x, im = a.y;      // phase * amplitude
-            a.x = R::sub(R::mul(k.c, re), R::mul(k.s, im));
-            a.y = R::add(R::mul(k.c, im), R::mul(k.s, re));
+    const unsigned pt = CPAT == PAT_RUNTIME ? pat : CPAT;
+    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < count; j += ITEMS * stride) {
+        uint32_t slot[ITEMS];
+        cplx<T> a[ITEMS];
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++) {
+            if (j + r * stride < count) {
+                const uint32_t x = tab[j + r * stride];
+                uint32_t y;
+                if constexpr (K == NP_PHASE1 || K == NP_NEG1 || K == NP_RZ0)
+                    y = ins_bit(x, t1, 0) | addbits;
+                else
+                    y = ins00(x, t1, t2) | addbits;
+                slot[r] = rank_dev(rt, y);
+                a[r] = st[slot[r]];
+            }
         }
-        st[slot] = a;
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++) {
+            if (j + r * stride >= count) continue;
+            const unsigned em = (pt >> (4 * r)) & 3;
+            const T re = a[r].x, im = a[r].y;
+            if constexpr (K == NP_NEG1 || K == NP_CZ) {
+                a[r].x = R::mul(re, T(-1));
+                a[r].y = R::mul(im, T(-1));
+            } else if constexpr (K == NP_RZ0 || K == NP_CRZ01) {
+                // cos*re + sin*im, cos*im - sin*re
+                a[r].x = dot2<T, false>((em & 1) != 0, re, k.c, k.kc, im, k.s, k.ks);
+                a[r].y = dot2<T, true>((em & 2) != 0, im, k.c, k.kc, re, k.s, k.ks);
+            } else {
+                // phase * amplitude: cos*re - sin*im, cos*im + sin*re
+                a[r].x = dot2<T, true>((em & 1) != 0, re, k.c, k.kc, im, k.s, k.ks);
+                a[r].y = dot2<T, false>((em & 2) != 0, im, k.c, k.kc, re, k.s, k.ks);
+            }
+            st[slot[r]] = a[r];
+        }
     }
 }
 
 // Pair updates over table {n-2, w-1} (np/gates.cpp:236-415).
-template <class T, int K>
+template <class T, int K, unsigned CPAT = PAT_RUNTIME>
 __global__ void __launch_bounds__(256) k_np_pair(cplx<T> *__restrict__ st,
                                                  const uint32_t *__restrict__ tab, uint64_t count,
                                                  const uint32_t *__restrict__ rt, unsigned lo,
-                                                 unsigned hi, uint32_t b1, uint32_t b2, NPCoef<T> k)
+                                                 unsigned hi, uint32_t b1, uint32_t b2, Coef<T> k,
+                                                 unsigned pat)
 {
-    using R = rn<T>;
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
-    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < count; j += stride) {
-        const uint32_t base = ins00(tab[j], lo, hi);
-        const uint32_t s1 = rank_dev(rt, base | b1), s2 = rank_dev(rt, base | b2);
-        cplx<T> a0 = st[s1], a1 = st[s2], r0, r1;
-        if constexpr (K == NP_SWAP) {
-            r0 = a1;
-            r1 = a0;
-        } else if constexpr (K == NP_RX) {       // :316-321
-            r0.x = R::add(R::mul(a0.x, k.c), R::mul(a1.y, k.s));
-            r0.y = R::sub(R::mul(a0.y, k.c), R::mul(a1.x, k.s));
-            r1.x = R::add(R::mul(a1.x, k.c), R::mul(a0.y, k.s));
-            r1.y = R::sub(R::mul(a1.y, k.c), R::mul(a0.x, k.s));
-        } else if constexpr (K == NP_RY) {       // :366-371
-            r0.x = R::sub(R::mul(a0.x, k.c), R::mul(a1.x, k.s));
-            r0.y = R::sub(R::mul(a0.y, k.c), R::mul(a1.y, k.s));
-            r1.x = R::add(R::mul(a0.x, k.s), R::mul(a1.x, k.c));
-            r1.y = R::add(R::mul(a0.y, k.s), R::mul(a1.y, k.c));
-        } else {                                 // NP_H, :409-412
-            r0.x = R::div(R::add(a0.x, a1.x), k.c);
-            r0.y = R::div(R::add(a0.y, a1.y), k.c);
-            r1.x = R::div(R::sub(a0.x, a1.x), k.c);
-            r1.y = R::div(R::sub(a0.y, a1.y), k.c);
+    const unsigned pt = CPAT == PAT_RUNTIME ? pat : CPAT;
+    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < count; j += ITEMS * stride) {
+        uint32_t s1[ITEMS], s2[ITEMS];
+        cplx<T> a0[ITEMS], a1[ITEMS];
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++) {
+            if (j + r * stride < count) {
+                const uint32_t base = ins00(tab[j + r * stride], lo, hi);
+                s1[r] = rank_dev(rt, base | b1);
+                s2[r] = rank_dev(rt, base | b2);
+                a0[r] = st[s1[r]];
+                a1[r] = st[s2[r]];
+            }
         }
-        st[s1] = r0;
-        st[s2] = r1;
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++) {
+            if (j + r * stride >= count) continue;
+            const bool E0 = (pt >> (4 * r)) & 1, E1 = (pt >> (4 * r)) & 2;
+            const bool E2 = (pt >> (4 * r)) & 4, E3 = (pt >> (4 * r)) & 8;
+            const cplx<T> p = a0[r], q = a1[r];
+            cplx<T> r0, r1;
+            if constexpr (K == NP_SWAP) {
+                r0 = q;
+                r1 = p;
+            } else if constexpr (K == NP_RX) {       // :316-321
+                r0.x = dot2<T, false>(E0, p.x, k.c, k.kc, q.y, k.s, k.ks);
+                r0.y = dot2<T, true>(E1, p.y, k.c, k.kc, q.x, k.s, k.ks);
+                r1.x = dot2<T, false>(E2, q.x, k.c, k.kc, p.y, k.s, k.ks);
+                r1.y = dot2<T, true>(E3, q.y, k.c, k.kc, p.x, k.s, k.ks);
+            } else if constexpr (K == NP_RY) {       // :366-371
+                r0.x = dot2<T, true>(E0, p.x, k.c, k.kc, q.x, k.s, k.ks);
+                r0.y = dot2<T, true>(E1, p.y, k.c, k.kc, q.y, k.s, k.ks);
+                r1.x = dot2<T, false>(E2, p.x, k.s, k.ks, q.x, k.c, k.kc);
+                r1.y = dot2<T, false>(E3, p.y, k.s, k.ks, q.y, k.c, k.kc);
+            } else {                                 // NP_H, :409-412
+                r0.x = hdiv<T, false>(E0, p.x, q.x, k);
+                r0.y = hdiv<T, false>(E1, p.y, q.y, k);
+                r1.x = hdiv<T, true>(E2, p.x, q.x, k);
+                r1.y = hdiv<T, true>(E3, p.y, q.y, k);
+            }
+            st[s1[r]] = r0;
+            st[s2[r]] = r1;
+        }
     }
 }
 
@@ -332,21 +363,39 @@ static int np_gate_t(qslc_state *s, int gate, unsigned q1, unsigned q2, double a
     const unsigned w = s->nones;
     cudaStream_t str = s->stream;
     const T a = T(angle);
-    auto single = [&](auto kind_tag, int ti, unsigned t1, unsigned t2, uint32_t add, NPCoef<T> k) {
+    auto single = [&](auto kind_tag, int ti, unsigned t1, unsigned t2, uint32_t add, Coef<T> k) {
         constexpr int KIND = decltype(kind_tag)::value;
         const uint64_t cnt = tb->len[ti];
         if (cnt == 0) return;
-        k_np_single<T, KIND><<<grid_for(cnt), 256, 0, str>>>(st, tb->tab[ti], cnt, rt, t1, t2, add, k);
+        const unsigned pat = sizeof(T) == 8 ? pattern_np_diag() : 0u;
+        auto go = [&](auto c) {
+            k_np_single<T, KIND, decltype(c)::value><<<grid_for(cnt), 256, 0, str>>>(st, tb->tab[ti], cnt, rt,
+                                                                                     t1, t2, add, k, pat);
+        };
+        if constexpr (KIND == NP_NEG1 || KIND == NP_CZ)
+            go(std::integral_constant<unsigned, 0u>{});
+        else
+            with_pattern<QSLC_NP_DIAG_PATTERNS>(pat, go);
         s->launches++;
     };
-    auto pair = [&](auto kind_tag, NPCoef<T> k) {
+    auto pair = [&](auto kind_tag, Coef<T> k) {
         constexpr int KIND = decltype(kind_tag)::value;
         const uint64_t cnt = tb->len[T_N2W1];
         if (cnt == 0) return;
         const unsigned lo = q1 < q2 ? q1 : q2, hi = q1 < q2 ? q2 : q1;
         uint32_t b1 = 1u << q1, b2 = 1u << q2;
         if (KIND == NP_SWAP) { b1 = 1u << lo; b2 = 1u << hi; }   // :259-260
-        k_np_pair<T, KIND><<<grid_for(cnt), 256, 0, str>>>(st, tb->tab[T_N2W1], cnt, rt, lo, hi, b1, b2, k);
+        const unsigned pat = sizeof(T) != 8 ? 0u : (KIND == NP_H ? pattern_h() : pattern_np_pair());
+        auto go = [&](auto c) {
+            k_np_pair<T, KIND, decltype(c)::value><<<grid_for(cnt), 256, 0, str>>>(
+                st, tb->tab[T_N2W1], cnt, rt, lo, hi, b1, b2, k, pat);
+        };
+        if constexpr (KIND == NP_SWAP)
+            go(std::integral_constant<unsigned, 0u>{});
+        else if constexpr (KIND == NP_H)
+            with_pattern<QSLC_H_PATTERNS>(pat, go);
+        else
+            with_pattern<QSLC_NP_PAIR_PATTERNS>(pat, go);
         s->launches++;
     };
     const unsigned lo = q1 < q2 ? q1 : q2, hi = q1 < q2 ? q2 : q1;
@@ -354,53 +403,53 @@ static int np_gate_t(qslc_state *s, int gate, unsigned q1, unsigned q2, double a
     switch (gate) {
     case QSLC_PHASE:       // np/gates.cpp:33-57
         single(std::integral_constant<int, NP_PHASE1>{}, T_N1W1, q1, 0, 1u << q1,
-               NPCoef<T>{T(std::cos(a)), T(std::sin(a))});
+               coef<T>(T(std::cos(a)), T(std::sin(a))));
         break;
     case QSLC_PAULI_Z:     // :59-80
-        single(std::integral_constant<int, NP_NEG1>{}, T_N1W1, q1, 0, 1u << q1, NPCoef<T>{});
+        single(std::integral_constant<int, NP_NEG1>{}, T_N1W1, q1, 0, 1u << q1, Coef<T>{});
         break;
     case QSLC_ROTATE_Z: {  // :83-113: e^{-ia/2} on |0>, then phase(a/2)
         single(std::integral_constant<int, NP_RZ0>{}, T_N1W, q1, 0, 0u,
-               NPCoef<T>{T(std::cos(a / 2)), T(std::sin(a / 2))});
+               coef<T>(T(std::cos(a / 2)), T(std::sin(a / 2))));
         const T h = a / 2;
         single(std::integral_constant<int, NP_PHASE1>{}, T_N1W1, q1, 0, 1u << q1,
-               NPCoef<T>{T(std::cos(h)), T(std::sin(h))});
+               coef<T>(T(std::cos(h)), T(std::sin(h))));
         break;
     }
     case QSLC_CONTROL_Z:   // :118-151
         if (w >= 2)
-            single(std::integral_constant<int, NP_CZ>{}, T_N2W2, lo, hi, both, NPCoef<T>{});
+            single(std::integral_constant<int, NP_CZ>{}, T_N2W2, lo, hi, both, Coef<T>{});
         break;
     case QSLC_CONTROL_PHASE:   // :195-233
         if (w >= 2)
             single(std::integral_constant<int, NP_CPHASE>{}, T_N2W2, lo, hi, both,
-                   NPCoef<T>{T(std::cos(a)), T(std::sin(a))});
+                   coef<T>(T(std::cos(a)), T(std::sin(a))));
         break;
     case QSLC_CONTROL_ROTATE_Z: {  // :154-192, q1 = control
         single(std::integral_constant<int, NP_CRZ01>{}, T_N2W1, lo, hi, 1u << q1,
-               NPCoef<T>{T(std::cos(a / 2)), T(std::sin(a / 2))});
+               coef<T>(T(std::cos(a / 2)), T(std::sin(a / 2))));
         const T h = a / 2;
         if (w >= 2)
             single(std::integral_constant<int, NP_CPHASE>{}, T_N2W2, lo, hi, both,
-                   NPCoef<T>{T(std::cos(h)), T(std::sin(h))});
+                   coef<T>(T(std::cos(h)), T(std::sin(h))));
         break;
     }
     case QSLC_SWAP:
-        pair(std::integral_constant<int, NP_SWAP>{}, NPCoef<T>{});
+        pair(std::integral_constant<int, NP_SWAP>{}, Coef<T>{});
         break;
     case QSLC_FSWAP:       // :267-275: swap, then controlZ
-        pair(std::integral_constant<int, NP_SWAP>{}, NPCoef<T>{});
+        pair(std::integral_constant<int, NP_SWAP>{}, Coef<T>{});
         if (w >= 2)
-            single(std::integral_constant<int, NP_CZ>{}, T_N2W2, lo, hi, both, NPCoef<T>{});
+            single(std::integral_constant<int, NP_CZ>{}, T_N2W2, lo, hi, both, Coef<T>{});
         break;
     case QSLC_NP_ROTATE_X:
-        pair(std::integral_constant<int, NP_RX>{}, NPCoef<T>{T(std::cos(a / 2)), T(std::sin(a / 2))});
+        pair(std::integral_constant<int, NP_RX>{}, coef<T>(T(std::cos(a / 2)), T(std::sin(a / 2))));
         break;
     case QSLC_NP_ROTATE_Y:
-        pair(std::integral_constant<int, NP_RY>{}, NPCoef<T>{T(std::cos(a / 2)), T(std::sin(a / 2))});
+        pair(std::integral_constant<int, NP_RY>{}, coef<T>(T(std::cos(a / 2)), T(std::sin(a / 2))));
         break;
     case QSLC_NP_HADAMARD:
-        pair(std::integral_constant<int, NP_H>{}, NPCoef<T>{T(std::sqrt(2)), T(0)});
+        pair(std::integral_constant<int, NP_H>{}, sqrt2_coef<T>());
         break;
     default:
         return fail(QSLC_EINVAL, "gate " + std::to_string(gate) +

@@ -65,3 +65,44 @@ def test_every_emulation_split_is_exact(qsl, port, tmp_path, rot, had, diag):
     for g, a, b, x in zip(names, q1, q2, ang):
         cpu.gate(str(g), int(a), None if int(b) < 0 else int(b), float(x))
     assert np.array_equal(bits(np.load(out)), bits(cpu.state))
+
+
+NP_SCRIPT = r"""
+import sys, numpy as np
+sys.path.insert(0, {root!r})
+import qsl_gb300 as q
+d = np.load({inp!r})
+sim = q.QubitsNP(state=d["state"])
+for g, a, b, x in zip(d["names"], d["q1"], d["q2"], d["ang"]):
+    sim.gate(str(g), int(a), None if int(b) < 0 else int(b), float(x))
+np.save({out!r}, sim.getState())
+"""
+NP_GATES = ("phase", "rotateZ", "controlPhase", "controlRotateZ", "npRotateX", "npRotateY",
+            "npHadamard")
+
+
+@pytest.mark.parametrize("pair,diag,had", [("0", "0", "0"), ("15", "3", "15"), ("5,1,1", "1,0,0", "0"),
+                                           ("6,9,3", "2,3,1", "5")])
+def test_np_emulation_splits_are_exact(qsl, port, tmp_path, pair, diag, had):
+    from conftest import random_np_state
+    rng = np.random.default_rng(len(pair) + 3 * len(diag))
+    n, w = 12, 5
+    st = random_np_state(rng, n, w)
+    names, q1, q2, ang = [], [], [], []
+    for _ in range(8):
+        for g in NP_GATES:
+            a, b = (int(v) for v in rng.choice(n, 2, replace=False))
+            names.append(g)
+            q1.append(a)
+            q2.append(-1 if g in ("phase", "rotateZ") else b)
+            ang.append(float(rng.uniform(0, 2 * np.pi)))
+    inp, out = str(tmp_path / "in.npz"), str(tmp_path / "out.npy")
+    np.savez(inp, state=st, names=np.array(names), q1=np.array(q1), q2=np.array(q2), ang=np.array(ang))
+    env = dict(os.environ, QSLC_EMU_MASK_NP=pair, QSLC_EMU_MASK_NP_DIAG=diag, QSLC_EMU_MASK_H=had)
+    r = subprocess.run([sys.executable, "-c", NP_SCRIPT.format(root=ROOT, inp=inp, out=out)],
+                       env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    cpu = port.PortNPQubits(n, w, state=st)
+    for g, a, b, x in zip(names, q1, q2, ang):
+        cpu.gate(g, a, None if b < 0 else b, x)
+    assert np.array_equal(bits(np.load(out)), bits(cpu.state))
