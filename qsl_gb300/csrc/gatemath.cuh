@@ -25,6 +25,36 @@ struct Coef {
     emu::DivConst kd;       // c as a divisor (Hadamard)
 };
 
+// FP64 arithmetic that the compiler may not execute speculatively.  The
+// fallback of an emulated output runs only for the operands the integer path
+// declines; written as ordinary arithmetic, a few FP64 instructions are cheap
+// enough that the compiler predicates them instead of branching, and then
+// every thread spends the FP64 pipe on them and the emulation saves nothing.
+__device__ __forceinline__ double dmul_ns(double a, double b)
+{
+    double r;
+    asm volatile("mul.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
+    return r;
+}
+__device__ __forceinline__ double dadd_ns(double a, double b)
+{
+    double r;
+    asm volatile("add.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
+    return r;
+}
+__device__ __forceinline__ double dsub_ns(double a, double b)
+{
+    double r;
+    asm volatile("sub.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
+    return r;
+}
+__device__ __forceinline__ double ddiv_ns(double a, double b)
+{
+    double r;
+    asm volatile("div.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
+    return r;
+}
+
 // One Hadamard output, RN(RN(a +- b) / sqrt2) (gates.cpp:95-98).  The
 // division always runs on the integer pipes (an FP64 divide is a long
 // iteration on the FP64 pipe); with `em` set the sum does too.
@@ -47,8 +77,10 @@ __device__ __forceinline__ T hdiv(bool em, T a, T b, const Coef<T> &k)
             const uint64_t q = emu::div_unp(sum, k.kd, ok);
             if (ok) return emu::dfrom(q);
         }
+        return ddiv_ns(NEG ? dsub_ns(a, b) : dadd_ns(a, b), k.c);
+    } else {
+        return R::div(NEG ? R::sub(a, b) : R::add(a, b), k.c);
     }
-    return R::div(NEG ? R::sub(a, b) : R::add(a, b), k.c);
 }
 
 // One output of a rotation or phase update: RN(RN(a*k1) + RN(b*k2)), or
@@ -60,10 +92,12 @@ __device__ __forceinline__ T dot2(bool em, T a, T k1, const emu::MulConst &e1, T
                                   const emu::MulConst &e2)
 {
     if constexpr (sizeof(T) == 8) {
-        bool ok = em && (e1.usable & e2.usable) != 0;
-        if (ok) {
+        if (em) {
+            bool ok = (e1.usable & e2.usable) != 0;
             const uint64_t r = emu::dot2_rn(emu::dbits(a), e1, emu::dbits(b), e2, NEG, ok);
             if (ok) return emu::dfrom(r);
+            const double p = dmul_ns(a, k1), q = dmul_ns(b, k2);
+            return NEG ? dsub_ns(p, q) : dadd_ns(p, q);
         }
     }
     using R = rn<T>;
