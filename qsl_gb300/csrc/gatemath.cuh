@@ -25,34 +25,24 @@ struct Coef {
     emu::DivConst kd;       // c as a divisor (Hadamard)
 };
 
-// FP64 arithmetic that the compiler may not execute speculatively.  The
-// fallback of an emulated output runs only for the operands the integer path
-// declines; written as ordinary arithmetic, a few FP64 instructions are cheap
-// enough that the compiler predicates them instead of branching, and then
-// every thread spends the FP64 pipe on them and the emulation saves nothing.
-__device__ __forceinline__ double dmul_ns(double a, double b)
+// The FP64 fallbacks of the emulated outputs, out of line.  They run only
+// for the operands the integer path declines (subnormals, infinities, NaNs,
+// results outside the normal range).  Inline, a fallback of a few FP64
+// instructions is cheap enough that the compiler predicates it instead of
+// branching around it; predicated FP64 instructions still take their turn
+// on the FP64 pipe, so every thread would pay for them and the emulation
+// would save nothing.  A call is not turned into predicated arithmetic:
+// measured on GB300, the inline forms ran the emulated patterns at the
+// all-FP64 speed, the out-of-line form at the speed the pattern predicts.
+template <bool NEG>
+__device__ __noinline__ double dot2_fallback(double a, double k1, double b, double k2)
 {
-    double r;
-    asm volatile("mul.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
-    return r;
+    return NEG ? __dsub_rn(__dmul_rn(a, k1), __dmul_rn(b, k2)) : __dadd_rn(__dmul_rn(a, k1), __dmul_rn(b, k2));
 }
-__device__ __forceinline__ double dadd_ns(double a, double b)
+template <bool NEG>
+__device__ __noinline__ double hdiv_fallback(double a, double b, double d)
 {
-    double r;
-    asm volatile("add.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
-    return r;
-}
-__device__ __forceinline__ double dsub_ns(double a, double b)
-{
-    double r;
-    asm volatile("sub.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
-    return r;
-}
-__device__ __forceinline__ double ddiv_ns(double a, double b)
-{
-    double r;
-    asm volatile("div.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
-    return r;
+    return __ddiv_rn(NEG ? __dsub_rn(a, b) : __dadd_rn(a, b), d);
 }
 
 // One Hadamard output, RN(RN(a +- b) / sqrt2) (gates.cpp:95-98).  The
@@ -77,7 +67,7 @@ __device__ __forceinline__ T hdiv(bool em, T a, T b, const Coef<T> &k)
             const uint64_t q = emu::div_unp(sum, k.kd, ok);
             if (ok) return emu::dfrom(q);
         }
-        return ddiv_ns(NEG ? dsub_ns(a, b) : dadd_ns(a, b), k.c);
+        return hdiv_fallback<NEG>(a, b, k.c);
     } else {
         return R::div(NEG ? R::sub(a, b) : R::add(a, b), k.c);
     }
@@ -95,9 +85,8 @@ __device__ __forceinline__ T dot2(bool em, T a, T k1, const emu::MulConst &e1, T
         if (em) {
             bool ok = (e1.usable & e2.usable) != 0;
             const uint64_t r = emu::dot2_rn(emu::dbits(a), e1, emu::dbits(b), e2, NEG, ok);
-            if (ok) return emu::dfrom(r);
-            const double p = dmul_ns(a, k1), q = dmul_ns(b, k2);
-            return NEG ? dsub_ns(p, q) : dadd_ns(p, q);
+if (ok) return emu::dfrom(r);
+            return dot2_fallback<NEG>(a, k1, b, k2);
         }
     }
     using R = rn<T>;
@@ -197,7 +186,7 @@ inline unsigned parse_pattern(const char *var, const char *dflt, unsigned width_
 }
 inline unsigned pattern_rot()
 {
-    static unsigned p = parse_pattern("QSLC_EMU_MASK", "5,1,1", 15);
+    static unsigned p = parse_pattern("QSLC_EMU_MASK", "5,5,1", 15);
     return p;
 }
 inline unsigned pattern_h()
