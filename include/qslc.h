@@ -260,6 +260,19 @@ QSLC_API int qslc_batch_create(int dtype, uint32_t ninst, const uint32_t *nqubit
  * order of the uniforms. */
 QSLC_API int qslc_batch_run(qslc_batch *b, const double *angles, const double *uniforms,
                             double *probs, uint64_t *shots);
+/* Measure every launch shape (threads per CTA, shared-memory tile of 64 or
+ * 128 KB, CTAs per SM) on this batch with these inputs and keep the fastest;
+ * best_ms receives its time for one run.  No reference counterpart. */
+QSLC_API int qslc_batch_autotune(qslc_batch *b, const double *angles, const double *uniforms,
+                                 double *best_ms);
+/* Use one launch shape; QSLC_EINVAL unless it is one the autotuner would
+ * try for this batch. */
+QSLC_API int qslc_batch_set_shape(qslc_batch *b, unsigned threads, unsigned tile_log2,
+                                  unsigned ctas_per_sm);
+/* The launch shape in use: threads per CTA, log2 of the tile's amplitudes,
+ * CTAs per SM and the grid. */
+QSLC_API int qslc_batch_shape(const qslc_batch *b, unsigned *threads, unsigned *tile_log2,
+                              unsigned *ctas_per_sm, unsigned *grid);
 QSLC_API int qslc_batch_destroy(qslc_batch *b);
 
 /* No counterpart in the reference: prob(targ, outcome) for callers that

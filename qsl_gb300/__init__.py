@@ -86,6 +86,10 @@ SIGNATURES = {
                                     C.POINTER(C.c_void_p)]),
     "qslc_batch_run": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
     "qslc_batch_destroy": (C.c_int, [_VP]),
+    "qslc_batch_autotune": (C.c_int, [_VP, _VP, _VP, C.POINTER(C.c_double)]),
+    "qslc_batch_set_shape": (C.c_int, [_VP, C.c_uint, C.c_uint, C.c_uint]),
+    "qslc_batch_shape": (C.c_int, [_VP, C.POINTER(C.c_uint), C.POINTER(C.c_uint),
+                                   C.POINTER(C.c_uint), C.POINTER(C.c_uint)]),
 }
 
 
@@ -447,3 +451,31 @@ class Batch:
             out.append(probs[at:at + 2 * n].reshape(n, 2))
             at += 2 * n
         return out, shots.reshape(self.n.size, self.nshots)
+
+    def autotune(self, angles, uniforms) -> float:
+        """Time every launch shape on these inputs, keep the fastest; returns
+        its milliseconds per run."""
+        a = np.ascontiguousarray(angles, dtype=np.float64)
+        u = np.ascontiguousarray(uniforms, dtype=np.float64)
+        ms = C.c_double()
+        _check(self.L.qslc_batch_autotune(self.h, _ptr(a), _ptr(u), C.byref(ms)))
+        return ms.value
+
+    def set_shape(self, threads: int, tile_log2: int, ctas_per_sm: int) -> None:
+        _check(self.L.qslc_batch_set_shape(self.h, threads, tile_log2, ctas_per_sm))
+
+    def shape(self) -> dict:
+        v = [C.c_uint() for _ in range(4)]
+        _check(self.L.qslc_batch_shape(self.h, *(C.byref(x) for x in v)))
+        return dict(zip(("threads", "tile_log2", "ctas_per_sm", "grid"), (x.value for x in v)))
+
+    def shapes(self) -> list:
+        """The launch shapes the autotuner tries for this batch."""
+        k = 13 if self.code == C128 else 14
+        out = []
+        for th in (512, 1024):
+            for tl, c in ((k - 1, 2), (k - 1, 1), (k, 1)):
+                if th * c > 1024 or int(self.n.max()) > 2 * tl:
+                    continue
+                out.append((th, tl, c))
+        return out

@@ -6,19 +6,31 @@
 // for q = 0..n-2; afterwards prob(q, 0) and prob(q, 1) for every q and a
 // sampleAll draw per uniform.  The per-instance result is the one qsl's
 // Default backend gives for the same calls (gates.cpp, measure.cpp), bit
-// for bit: the gates run in the reference's order with its rounding, the
-// probabilities are sequential sums in index order, and the sampling CDF is
-// the sequential double sum merged against the instance's sorted uniforms
-// (the first index whose running sum reaches a uniform is its outcome, as
-// drawSample's search returns, measure.cpp:164-188).
+// for bit: every amplitude sees the reference's operations in the
+// reference's order with its rounding, the probabilities are sequential
+// sums in index order, and the sampling CDF is the sequential double sum
+// merged against the instance's sorted uniforms (the first index whose
+// running sum reaches a uniform is its outcome, as drawSample's search
+// returns, measure.cpp:164-188).
 //
-// Schedule: one CTA of 1024 threads per resident slot pulls instances,
-// largest first, from an atomic counter.  A state of up to SMEM_STATE bytes
-// lives in shared memory for its whole circuit and never touches HBM; a
-// larger one works in the CTA's slot of a global arena (L2 / HBM).  The
-// probabilities use n threads (one sequential sum per qubit) and the CDF
-// one more thread, running side by side.
-#include "qslc_internal.cuh"
+// Schedule: persistent CTAs pull instances, largest first, from an atomic
+// counter.  A state of at most one tile (2^k amplitudes of shared memory)
+// lives in shared memory for its whole circuit.  A larger state lives in
+// two buffers of the CTA's slot in a global arena and takes two passes per
+// layer instead of one per gate:
+//   pass 1  tiles of 2^k consecutive amplitudes: rotateY on qubits 0..k-1;
+//   pass 2  tiles that vary the high n-k qubits and the lowest 2k-n ones:
+//           rotateY on qubits k..n-1, then rotateZ on every qubit (each
+//           rotateZ touches one amplitude at a time, so all n of them apply
+//           per amplitude, in order), then the whole controlNot ladder as
+//           one permutation into the other buffer.
+// The ladder maps basis index x to y with y_i = x_0 ^ ... ^ x_i (each
+// controlNot(q, q+1) flips bit q+1 when bit q of the running index is set);
+// a pass-2 tile writes its outputs in runs of consecutive y.
+//
+// The tile size, threads per CTA and CTAs per SM are picked by measuring
+// the candidates on the caller's own batch (qslc_batch_autotune).
+#include "gatemath.cuh"
 #include "replay.cuh"
 
 #include <algorithm>
@@ -29,8 +41,12 @@
 namespace qslc {
 namespace {
 
-constexpr int BATCH_THREADS = 1024;
-constexpr size_t SMEM_STATE = 128 * 1024;
+constexpr int MAX_Q = 26;
+// Share of the rotation outputs on the integer pipes (complex128), cycled
+// over a thread's successive pairs: two of four, two of four, one of four;
+// and for rotateZ over the qubits: one of two, one of two, none.
+constexpr unsigned BATCH_PAT_RY = 0x155u;
+constexpr unsigned BATCH_PAT_RZ = 0x011u;
 
 struct InstDesc {
     uint32_t n, L;
@@ -39,87 +55,109 @@ struct InstDesc {
     uint64_t shots;     // offset of its shots (sorted-uniform order)
 };
 
+struct BatchArgs {
+    const InstDesc *inst;
+    const uint32_t *order;
+    uint32_t ninst;
+    unsigned *counter;
+    const void *coef;
+    void *probs;
+    const double *usorted;
+    uint64_t *shots;
+    uint32_t nshots;
+    void *arena;
+    uint64_t slot_amps;     // amplitudes per arena buffer (two buffers per slot)
+    unsigned tile_log2;     // k: the shared-memory tile holds 2^k amplitudes
+};
+
+__host__ __device__ __forceinline__ uint64_t ladder(uint64_t x)
+{   // y_i = x_0 ^ ... ^ x_i
+    x ^= x << 1;
+    x ^= x << 2;
+    x ^= x << 4;
+    x ^= x << 8;
+    x ^= x << 16;
+    return x;
+}
+
+// The coefficients of one layer, decoded for the integer path once per CTA.
 template <class T>
-__device__ __forceinline__ void ry_pair(cplx<T> &a0, cplx<T> &a1, T c, T s)
-{   // gates.cpp:169-174
-    using R = rn<T>;
-    cplx<T> r0, r1;
-    r0.x = R::sub(R::mul(a0.x, c), R::mul(a1.x, s));
-    r0.y = R::sub(R::mul(a0.y, c), R::mul(a1.y, s));
-    r1.x = R::add(R::mul(a0.x, s), R::mul(a1.x, c));
-    r1.y = R::add(R::mul(a0.y, s), R::mul(a1.y, c));
-    a0 = r0;
-    a1 = r1;
+struct LayerCoefs {
+    Coef<T> ry[MAX_Q], rz[MAX_Q];
+};
+
+template <class T>
+__device__ __forceinline__ Coef<T> dev_coef(T c, T s)
+{
+    Coef<T> k{};
+    k.c = c;
+    k.s = s;
+    k.kc = emu::make_const(double(c));
+    k.ks = emu::make_const(double(s));
+    return k;
 }
 
 template <class T>
-__device__ __forceinline__ void rz_pair(cplx<T> &a0, cplx<T> &a1, T c, T s)
-{   // gates.cpp:200-205
-    using R = rn<T>;
-    cplx<T> r0, r1;
-    r0.x = R::add(R::mul(a0.x, c), R::mul(a0.y, s));
-    r0.y = R::sub(R::mul(a0.y, c), R::mul(a0.x, s));
-    r1.x = R::sub(R::mul(a1.x, c), R::mul(a1.y, s));
-    r1.y = R::add(R::mul(a1.y, c), R::mul(a1.x, s));
-    a0 = r0;
-    a1 = r1;
+__device__ __forceinline__ void stage_layer(LayerCoefs<T> &lc, const T *cf, uint32_t n)
+{
+    const unsigned tid = threadIdx.x;
+    if (tid < n) {
+        lc.ry[tid] = dev_coef<T>(cf[4 * tid], cf[4 * tid + 1]);
+        lc.rz[tid] = dev_coef<T>(cf[4 * tid + 2], cf[4 * tid + 3]);
+    }
+    __syncthreads();
 }
 
+// rotateY on qubit `bit` of a state or tile held at `st` (2^m amplitudes),
+// gates.cpp:169-174; every thread's pairs cycle through BATCH_PAT_RY.
 template <class T>
-__device__ void run_instance(cplx<T> *st, const InstDesc &d, const T *__restrict__ coef,
-                             T *__restrict__ probs, const double *__restrict__ u_sorted,
-                             uint64_t *__restrict__ shots, uint32_t nshots)
+__device__ __forceinline__ void ry_sweep(cplx<T> *st, unsigned m, unsigned bit, const Coef<T> &k)
+{
+    const uint64_t half = uint64_t(1) << (m - 1), b = uint64_t(1) << bit;
+    unsigned it = 0;
+    for (uint64_t j = threadIdx.x; j < half; j += blockDim.x, it = (it == 2 ? 0 : it + 1)) {
+        const uint64_t i0 = insert0(j, bit);
+        cplx<T> a0 = st[i0], a1 = st[i0 | b];
+        pair_update<T, P_RY>(a0, a1, k, (BATCH_PAT_RY >> (4 * it)) & 15);
+        st[i0] = a0;
+        st[i0 | b] = a1;
+    }
+}
+
+// rotateZ on qubits 0..n-1, in that order, of the amplitude at basis index
+// x (gates.cpp:200-205): the |0> member takes (re*c + im*s, im*c - re*s),
+// the |1> member (re*c - im*s, im*c + re*s).  Both are re*c + im*sg and
+// im*c + re*(-sg) with sg = +-s, and RN(u*(-v)) = -RN(u*v), so one form
+// serves both members without a branch on the bit.
+template <class T>
+__device__ __forceinline__ cplx<T> rz_all(cplx<T> a, uint64_t x, uint32_t n, const LayerCoefs<T> &lc)
+{
+    for (uint32_t q = 0; q < n; q++) {
+        const Coef<T> &k = lc.rz[q];
+        const bool one = (x >> q) & 1;
+        const T sg = one ? -k.s : k.s;
+        emu::MulConst ksg = k.ks, kneg = k.ks;
+        if (one) ksg.sign ^= emu::SIGN;
+        else kneg.sign ^= emu::SIGN;
+        const unsigned em = (BATCH_PAT_RZ >> (4 * (q % 3))) & 3;
+        const T re = a.x, im = a.y;
+        a.x = dot2<T, false>((em & 1) != 0, re, k.c, k.kc, im, sg, ksg);
+        a.y = dot2<T, false>((em & 2) != 0, im, k.c, k.kc, re, -sg, kneg);
+    }
+    return a;
+}
+
+// The measurements of one instance from its final state `st` (shared or
+// global memory, natural order).
+template <class T>
+__device__ void finish_instance(const cplx<T> *st, const InstDesc &d, T *__restrict__ probs,
+                                const double *__restrict__ u, uint64_t *__restrict__ shots,
+                                uint32_t nshots)
 {
     const uint32_t n = d.n;
     const uint64_t dim = uint64_t(1) << n, half = dim >> 1;
-    const unsigned tid = threadIdx.x, nt = blockDim.x;
-    for (uint64_t i = tid; i < dim; i += nt) {
-        cplx<T> z;
-        z.x = T(i == 0 ? 1 : 0);
-        z.y = T(0);
-        st[i] = z;
-    }
-    __syncthreads();
-    const T *cf = coef + d.coef;
-    for (uint32_t l = 0; l < d.L; l++) {
-        const T *lc = cf + uint64_t(l) * n * 4;
-        for (uint32_t q = 0; q < n; q++) {           // rotateY on every qubit
-            const T c = lc[4 * q], s = lc[4 * q + 1];
-            const uint64_t bit = uint64_t(1) << q;
-            for (uint64_t j = tid; j < half; j += nt) {
-                uint64_t i0 = insert0(j, q);
-                cplx<T> a0 = st[i0], a1 = st[i0 | bit];
-                ry_pair<T>(a0, a1, c, s);
-                st[i0] = a0;
-                st[i0 | bit] = a1;
-            }
-            __syncthreads();
-        }
-        for (uint32_t q = 0; q < n; q++) {           // rotateZ on every qubit
-            const T c = lc[4 * q + 2], s = lc[4 * q + 3];
-            const uint64_t bit = uint64_t(1) << q;
-            for (uint64_t j = tid; j < half; j += nt) {
-                uint64_t i0 = insert0(j, q);
-                cplx<T> a0 = st[i0], a1 = st[i0 | bit];
-                rz_pair<T>(a0, a1, c, s);
-                st[i0] = a0;
-                st[i0 | bit] = a1;
-            }
-            __syncthreads();
-        }
-        for (uint32_t q = 0; q + 1 < n; q++) {       // controlNot(q, q+1), gates.cpp:215-240
-            const uint64_t cb = uint64_t(1) << q, tb = uint64_t(1) << (q + 1);
-            for (uint64_t j = tid; j < (dim >> 2); j += nt) {
-                uint64_t x1 = insert00(j, q, q + 1) | cb;
-                cplx<T> a = st[x1], b = st[x1 | tb];
-                st[x1] = b;
-                st[x1 | tb] = a;
-            }
-            __syncthreads();
-        }
-    }
+    const unsigned tid = threadIdx.x;
     // prob(q, o): sequential Fp sums in index order (measure.cpp:126-147)
-    T *pr = probs + d.probs;
     if (tid < 2 * n) {
         const uint32_t q = tid >> 1, o = tid & 1;
         const uint64_t ob = uint64_t(o) << q;
@@ -128,18 +166,16 @@ __device__ void run_instance(cplx<T> *st, const InstDesc &d, const T *__restrict
             const cplx<T> a = st[insert0(j, q) | ob];
             p = rn<T>::add(p, norm2_rn(a.x, a.y));
         }
-        pr[2 * q + o] = p;
+        probs[d.probs + 2 * q + o] = p;
     } else if (tid == 2 * n) {
         // sampling: the double running sum over all amplitudes, merged
         // against the sorted uniforms (measure.cpp:60-78, :164-188)
-        const double *u = u_sorted;
         uint64_t *out = shots + d.shots;
         uint32_t k = 0;
         double run = 0.0;
         for (uint64_t i = 0; i < dim && k < nshots; i++) {
             const cplx<T> a = st[i];
-            const T p = norm2_rn(a.x, a.y);
-            run = __dadd_rn(run, double(p));
+            run = __dadd_rn(run, double(norm2_rn(a.x, a.y)));
             while (k < nshots && u[k] <= run) out[k++] = i;
         }
         for (; k < nshots; k++) out[k] = 0;           // above the total: index 0
@@ -147,31 +183,129 @@ __device__ void run_instance(cplx<T> *st, const InstDesc &d, const T *__restrict
     __syncthreads();
 }
 
+// An instance that fits one tile: the whole circuit in shared memory.
 template <class T>
-__global__ void __launch_bounds__(BATCH_THREADS) k_batch(const InstDesc *__restrict__ inst,
-                                                         const uint32_t *__restrict__ order,
-                                                         uint32_t ninst, unsigned *counter,
-                                                         const T *__restrict__ coef,
-                                                         T *__restrict__ probs,
-                                                         const double *__restrict__ usorted,
-                                                         uint64_t *__restrict__ shots,
-                                                         uint32_t nshots, cplx<T> *arena,
-                                                         uint64_t slot_amps)
+__device__ void run_small(cplx<T> *sm, LayerCoefs<T> &lc, const InstDesc &d, const T *coef)
+{
+    const uint32_t n = d.n;
+    const uint64_t dim = uint64_t(1) << n;
+    const unsigned tid = threadIdx.x, nt = blockDim.x;
+    for (uint64_t i = tid; i < dim; i += nt) {
+        cplx<T> z;
+        z.x = T(i == 0 ? 1 : 0);
+        z.y = T(0);
+        sm[i] = z;
+    }
+    for (uint32_t l = 0; l < d.L; l++) {
+        stage_layer<T>(lc, coef + d.coef + uint64_t(l) * n * 4, n);   // also orders the fill
+        for (uint32_t q = 0; q < n; q++) {
+            ry_sweep<T>(sm, n, q, lc.ry[q]);
+            __syncthreads();
+        }
+        for (uint64_t i = tid; i < dim; i += nt) sm[i] = rz_all<T>(sm[i], i, n, lc);
+        __syncthreads();
+        for (uint32_t q = 0; q + 1 < n; q++) {       // controlNot(q, q+1), gates.cpp:215-240
+            const uint64_t cb = uint64_t(1) << q, tb = uint64_t(1) << (q + 1);
+            for (uint64_t j = tid; j < (dim >> 2); j += nt) {
+                const uint64_t x1 = insert00(j, q, q + 1) | cb;
+                const cplx<T> a = sm[x1], b = sm[x1 | tb];
+                sm[x1] = b;
+                sm[x1 | tb] = a;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// An instance larger than a tile: two buffers in the CTA's arena slot, two
+// passes per layer.  Returns the buffer that holds the final state.
+template <class T>
+__device__ cplx<T> *run_big(cplx<T> *sm, LayerCoefs<T> &lc, const InstDesc &d, const T *coef,
+                            cplx<T> *buf0, cplx<T> *buf1, unsigned k)
+{
+    const uint32_t n = d.n;
+    const uint64_t dim = uint64_t(1) << n, tile = uint64_t(1) << k;
+    const unsigned tid = threadIdx.x, nt = blockDim.x;
+    const unsigned h = n - k;                 // qubits above the tile (h <= k)
+    const unsigned c = k - h;                 // low qubits that pass-2 tiles keep whole
+    const uint64_t cmask = (uint64_t(1) << c) - 1;
+    cplx<T> *src = buf0, *dst = buf1;
+    for (uint64_t i = tid; i < dim; i += nt) {
+        cplx<T> z;
+        z.x = T(i == 0 ? 1 : 0);
+        z.y = T(0);
+        src[i] = z;
+    }
+    for (uint32_t l = 0; l < d.L; l++) {
+        stage_layer<T>(lc, coef + d.coef + uint64_t(l) * n * 4, n);   // also orders the writes above
+        // pass 1: rotateY on qubits 0..k-1, tile by tile, in place
+        for (uint64_t t = 0; t < (dim >> k); t++) {
+            cplx<T> *g = src + (t << k);
+            for (uint64_t i = tid; i < tile; i += nt) sm[i] = g[i];
+            __syncthreads();
+            for (unsigned q = 0; q < k; q++) {
+                ry_sweep<T>(sm, k, q, lc.ry[q]);
+                __syncthreads();
+            }
+            for (uint64_t i = tid; i < tile; i += nt) g[i] = sm[i];
+            __syncthreads();
+        }
+        // pass 2: tile t fixes bits c..k-1 of the index to t; local index
+        // l = (high bits << c) | (low c bits)
+        for (uint64_t t = 0; t < (uint64_t(1) << h); t++) {
+            const uint64_t mid = t << c;
+            for (uint64_t i = tid; i < tile; i += nt) sm[i] = src[((i >> c) << k) | mid | (i & cmask)];
+            __syncthreads();
+            for (unsigned q = k; q < n; q++) {
+                ry_sweep<T>(sm, k, c + (q - k), lc.ry[q]);
+                __syncthreads();
+            }
+            // outputs in order of their destination: o = (high bits << c) |
+            // (low c bits of y); the source's low bits are the inverse of the
+            // ladder on those c bits, so consecutive o land on consecutive y
+            for (uint64_t o = tid; o < tile; o += nt) {
+                const uint64_t ylow = o & cmask;
+                const uint64_t xlow = (ylow ^ (ylow << 1)) & cmask;
+                const uint64_t lidx = (o & ~cmask) | xlow;
+                const uint64_t x = ((o >> c) << k) | mid | xlow;
+                dst[ladder(x) & (dim - 1)] = rz_all<T>(sm[lidx], x, n, lc);
+            }
+            __syncthreads();
+        }
+        cplx<T> *tmp = src;
+        src = dst;
+        dst = tmp;
+    }
+    return src;
+}
+
+template <class T>
+__global__ void __launch_bounds__(1024) k_batch(BatchArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint32_t next;
+    __shared__ LayerCoefs<T> lc;
     cplx<T> *sm = reinterpret_cast<cplx<T> *>(smem_raw);
+    const T *coef = static_cast<const T *>(a.coef);
+    T *probs = static_cast<T *>(a.probs);
+    cplx<T> *slot = static_cast<cplx<T> *>(a.arena) + uint64_t(blockIdx.x) * 2 * a.slot_amps;
     while (true) {
-        if (threadIdx.x == 0) next = atomicAdd(counter, 1u);
+        if (threadIdx.x == 0) next = atomicAdd(a.counter, 1u);
         __syncthreads();
         const uint32_t w = next;
         __syncthreads();
-        if (w >= ninst) break;
-        const uint32_t id = order[w];
-        const InstDesc d = inst[id];
-        const bool on_chip = (uint64_t(1) << d.n) * sizeof(cplx<T>) <= SMEM_STATE;
-        cplx<T> *st = on_chip ? sm : arena + uint64_t(blockIdx.x) * slot_amps;
-        run_instance<T>(st, d, coef, probs, usorted + uint64_t(id) * nshots, shots, nshots);
+        if (w >= a.ninst) break;
+        const uint32_t id = a.order[w];
+        const InstDesc d = a.inst[id];
+        const double *u = a.usorted + uint64_t(id) * a.nshots;
+        if (d.n <= a.tile_log2) {
+            run_small<T>(sm, lc, d, coef);
+            finish_instance<T>(sm, d, probs, u, a.shots, a.nshots);
+        } else {
+            const cplx<T> *fin = run_big<T>(sm, lc, d, coef, slot, slot + a.slot_amps, a.tile_log2);
+            __syncthreads();
+            finish_instance<T>(fin, d, probs, u, a.shots, a.nshots);
+        }
     }
 }
 
@@ -180,16 +314,24 @@ __global__ void __launch_bounds__(BATCH_THREADS) k_batch(const InstDesc *__restr
 
 using namespace qslc;
 
+// One launch shape of the persistent kernel.
+struct BatchShape {
+    unsigned threads = 1024;
+    unsigned tile_log2 = 13;
+    unsigned ctas_per_sm = 1;
+};
+
 struct qslc_batch {
     int dtype = QSLC_C128;
-    uint32_t ninst = 0, nshots = 0;
+    uint32_t ninst = 0, nshots = 0, nmax = 0;
     std::vector<InstDesc> inst;
     std::vector<uint32_t> order;
     uint64_t ncoef = 0, nprobs = 0, nshot_total = 0;
     cudaStream_t stream = nullptr;
     void *d_inst = nullptr, *d_order = nullptr, *d_counter = nullptr, *d_coef = nullptr;
     void *d_probs = nullptr, *d_u = nullptr, *d_shots = nullptr, *d_arena = nullptr;
-    uint64_t slot_amps = 0;
+    uint64_t arena_bytes = 0, slot_amps = 0;
+    BatchShape shape;
     unsigned grid = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -198,12 +340,25 @@ struct qslc_batch {
 
 namespace {
 
+// The arena holds two buffers of 2^nmax amplitudes per CTA; beyond this
+// many bytes the grid shrinks instead.
+constexpr uint64_t ARENA_CAP = uint64_t(64) << 30;
+
+size_t amp_bytes(int dtype) { return dtype == QSLC_C128 ? 16 : 8; }
+
+void drop_graph(qslc_batch *b)
+{
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+}
+
 void batch_free(qslc_batch *b)
 {
     if (!b) return;
     if (b->stream) cudaStreamSynchronize(b->stream);
-    if (b->exec) cudaGraphExecDestroy(b->exec);
-    if (b->graph) cudaGraphDestroy(b->graph);
+    drop_graph(b);
     for (void *p : {b->d_inst, b->d_order, b->d_counter, b->d_coef, b->d_probs, b->d_u, b->d_shots,
                     b->d_arena})
         if (p) cudaFree(p);
@@ -211,31 +366,81 @@ void batch_free(qslc_batch *b)
     delete b;
 }
 
-template <class T>
-int capture(qslc_batch *b)
+// Whether a shape can run this batch: the tile must fit a CTA's shared
+// memory and cover at least half of the largest instance's qubits.
+bool shape_fits(const qslc_batch *b, const BatchShape &s)
 {
-    const size_t smem = SMEM_STATE;
+    const size_t tile = (size_t(1) << s.tile_log2) * amp_bytes(b->dtype);
+    if (tile * s.ctas_per_sm + 16 * 1024 * s.ctas_per_sm > 224 * 1024) return false;
+    if (s.threads * s.ctas_per_sm > 1024) return false;   // registers: 64 K per SM, up to 64 a thread
+    if (b->nmax > 2 * s.tile_log2) return false;
+    return true;
+}
+
+// (Re)capture the graph for shape `s`: grid, arena size, kernel attributes.
+template <class T>
+int capture(qslc_batch *b, const BatchShape &s)
+{
+    drop_graph(b);
+    const size_t ab = amp_bytes(b->dtype);
+    const size_t smem = (size_t(1) << s.tile_log2) * ab;
+    b->slot_amps = b->nmax > s.tile_log2 ? (uint64_t(1) << b->nmax) : 0;
+    unsigned grid = sm_count() * s.ctas_per_sm;
+    if (b->slot_amps) {
+        const uint64_t slot = 2 * b->slot_amps * ab;
+        grid = unsigned(std::min<uint64_t>(grid, std::max<uint64_t>(1, ARENA_CAP / slot)));
+    }
+    grid = std::min<unsigned>(grid, b->ninst);
+    const uint64_t need = uint64_t(grid) * 2 * b->slot_amps * ab;
+    if (need > b->arena_bytes) {
+        if (b->d_arena) cudaFree(b->d_arena);
+        b->d_arena = nullptr;
+        b->arena_bytes = 0;
+        if (cudaMalloc(&b->d_arena, std::max<uint64_t>(need, 16)) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(QSLC_EOOM, "out of device memory for the batch arena");
+        }
+        b->arena_bytes = need;
+    }
     QSLC_CUDA(cudaFuncSetAttribute(k_batch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    BatchArgs a;
+    a.inst = static_cast<const InstDesc *>(b->d_inst);
+    a.order = static_cast<const uint32_t *>(b->d_order);
+    a.ninst = b->ninst;
+    a.counter = static_cast<unsigned *>(b->d_counter);
+    a.coef = b->d_coef;
+    a.probs = b->d_probs;
+    a.usorted = static_cast<const double *>(b->d_u);
+    a.shots = static_cast<uint64_t *>(b->d_shots);
+    a.nshots = b->nshots;
+    a.arena = b->d_arena;
+    a.slot_amps = b->slot_amps;
+    a.tile_log2 = s.tile_log2;
     QSLC_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned), b->stream);
-    k_batch<T><<<b->grid, BATCH_THREADS, smem, b->stream>>>(
-        static_cast<const InstDesc *>(b->d_inst), static_cast<const uint32_t *>(b->d_order), b->ninst,
-        static_cast<unsigned *>(b->d_counter), static_cast<const T *>(b->d_coef),
-        static_cast<T *>(b->d_probs), static_cast<const double *>(b->d_u),
-        static_cast<uint64_t *>(b->d_shots), b->nshots, static_cast<cplx<T> *>(b->d_arena), b->slot_amps);
+    k_batch<T><<<grid, s.threads, smem, b->stream>>>(a);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
     b->graph = g;
     QSLC_CUDA(cudaGraphInstantiate(&b->exec, g, 0));
+    b->shape = s;
+    b->grid = grid;
     return QSLC_OK;
 }
 
-template <class T>
-int run_t(qslc_batch *b, const double *angles, const double *u, double *probs, uint64_t *shots)
+int capture_any(qslc_batch *b, const BatchShape &s)
 {
-    // coefficients exactly as the reference computes them (gates.cpp:154-155,
-    // :185-186): Fp cos/sin of Fp(angle)/2
+    return b->dtype == QSLC_C128 ? capture<double>(b, s) : capture<float>(b, s);
+}
+
+// Coefficients exactly as the reference computes them (gates.cpp:154-155,
+// :185-186: Fp cos/sin of Fp(angle)/2) and each instance's uniforms sorted
+// (in Fp, as the reference draws them), uploaded; `perm` maps sorted
+// positions back to the caller's order.
+template <class T>
+int upload_inputs(qslc_batch *b, const double *angles, const double *u, std::vector<uint32_t> &perm)
+{
     std::vector<T> coef(b->ncoef);
     uint64_t a = 0;
     for (uint32_t i = 0; i < b->ninst; i++) {
@@ -250,10 +455,9 @@ int run_t(qslc_batch *b, const double *angles, const double *u, double *probs, u
         }
         a += 2 * uint64_t(d.L) * d.n;
     }
-    // sort each instance's uniforms; shots come back in sorted order
     const uint32_t ns = b->nshots;
     std::vector<double> us(uint64_t(b->ninst) * ns);
-    std::vector<uint32_t> perm(uint64_t(b->ninst) * ns);
+    perm.resize(uint64_t(b->ninst) * ns);
     for (uint32_t i = 0; i < b->ninst; i++) {
         uint32_t *pm = perm.data() + uint64_t(i) * ns;
         const double *ui = u + uint64_t(i) * ns;
@@ -267,7 +471,19 @@ int run_t(qslc_batch *b, const double *angles, const double *u, double *probs, u
     }
     QSLC_CUDA(cudaMemcpyAsync(b->d_coef, coef.data(), coef.size() * sizeof(T), cudaMemcpyHostToDevice, b->stream));
     QSLC_CUDA(cudaMemcpyAsync(b->d_u, us.data(), us.size() * 8, cudaMemcpyHostToDevice, b->stream));
-    QSLC_CUDA(cudaGraphLaunch(b->exec, b->stream));
+    QSLC_CUDA(cudaStreamSynchronize(b->stream));
+    return QSLC_OK;
+}
+
+int upload_any(qslc_batch *b, const double *angles, const double *u, std::vector<uint32_t> &perm)
+{
+    return b->dtype == QSLC_C128 ? upload_inputs<double>(b, angles, u, perm)
+                                 : upload_inputs<float>(b, angles, u, perm);
+}
+
+template <class T>
+int download(qslc_batch *b, const std::vector<uint32_t> &perm, double *probs, uint64_t *shots)
+{
     std::vector<T> pr(b->nprobs);
     std::vector<uint64_t> sh(b->nshot_total);
     QSLC_CUDA(cudaMemcpyAsync(pr.data(), b->d_probs, pr.size() * sizeof(T), cudaMemcpyDeviceToHost, b->stream));
@@ -275,11 +491,28 @@ int run_t(qslc_batch *b, const double *angles, const double *u, double *probs, u
     QSLC_CUDA(cudaStreamSynchronize(b->stream));
     QSLC_CUDA(cudaGetLastError());
     for (uint64_t i = 0; i < b->nprobs; i++) probs[i] = double(pr[i]);
+    const uint32_t ns = b->nshots;
     for (uint32_t i = 0; i < b->ninst; i++)
         for (uint32_t k = 0; k < ns; k++)
             shots[uint64_t(i) * ns + perm[uint64_t(i) * ns + k]] = sh[b->inst[i].shots + k];
-    b->runs++;
     return QSLC_OK;
+}
+
+// The launch shapes the autotuner measures: threads per CTA, a tile of
+// 64 or 128 KB, one or two CTAs per SM.
+std::vector<BatchShape> candidates(const qslc_batch *b)
+{
+    const unsigned k128 = b->dtype == QSLC_C128 ? 13 : 14;
+    std::vector<BatchShape> out;
+    for (unsigned th : {512u, 1024u})
+        for (const auto &tc : {std::pair<unsigned, unsigned>{k128 - 1, 2u}, {k128 - 1, 1u}, {k128, 1u}}) {
+            BatchShape s;
+            s.threads = th;
+            s.tile_log2 = tc.first;
+            s.ctas_per_sm = tc.second;
+            if (shape_fits(b, s)) out.push_back(s);
+        }
+    return out;
 }
 
 }  // namespace
@@ -295,9 +528,8 @@ extern "C" int qslc_batch_create(int dtype, uint32_t ninst, const uint32_t *nqub
     b->ninst = ninst;
     b->nshots = nshots;
     b->inst.resize(ninst);
-    uint32_t nmax = 0;
     for (uint32_t i = 0; i < ninst; i++) {
-        if (nqubits[i] < 2 || nqubits[i] > 26) {
+        if (nqubits[i] < 2 || nqubits[i] > uint32_t(MAX_Q)) {
             delete b;
             return fail(QSLC_EINVAL, "batch instances take 2..26 qubits");
         }
@@ -310,7 +542,7 @@ extern "C" int qslc_batch_create(int dtype, uint32_t ninst, const uint32_t *nqub
         b->ncoef += uint64_t(d.L) * d.n * 4;
         b->nprobs += 2 * uint64_t(d.n);
         b->nshot_total += nshots;
-        nmax = std::max(nmax, d.n);
+        b->nmax = std::max(b->nmax, d.n);
     }
     // largest instances first, so the long ones start early
     b->order.resize(ninst);
@@ -318,14 +550,11 @@ extern "C" int qslc_batch_create(int dtype, uint32_t ninst, const uint32_t *nqub
     std::stable_sort(b->order.begin(), b->order.end(), [&](uint32_t x, uint32_t y) {
         return (uint64_t(b->inst[x].L) << b->inst[x].n) > (uint64_t(b->inst[y].L) << b->inst[y].n);
     });
-    const size_t ab = dtype == QSLC_C128 ? 16 : 8, fb = dtype == QSLC_C128 ? 8 : 4;
-    b->grid = sm_count();
-    b->slot_amps = (uint64_t(1) << nmax) * ab > SMEM_STATE ? (uint64_t(1) << nmax) : 0;
+    const size_t fb = dtype == QSLC_C128 ? 8 : 4;
     int rc = QSLC_OK;
     auto alloc = [&](void **p, size_t bytes) {
         if (rc) return;
-        if (bytes == 0) bytes = 16;
-        if (cudaMalloc(p, bytes) != cudaSuccess) {
+        if (cudaMalloc(p, std::max<size_t>(bytes, 16)) != cudaSuccess) {
             cudaGetLastError();
             rc = fail(QSLC_EOOM, "out of device memory for the batch");
         }
@@ -337,14 +566,17 @@ extern "C" int qslc_batch_create(int dtype, uint32_t ninst, const uint32_t *nqub
     alloc(&b->d_probs, b->nprobs * fb);
     alloc(&b->d_u, b->nshot_total * 8);
     alloc(&b->d_shots, b->nshot_total * 8);
-    alloc(&b->d_arena, size_t(b->grid) * b->slot_amps * ab);
     if (!rc && cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess)
         rc = fail(QSLC_ECUDA, "stream creation failed");
     if (!rc && cudaMemcpy(b->d_inst, b->inst.data(), ninst * sizeof(InstDesc), cudaMemcpyHostToDevice) != cudaSuccess)
         rc = fail(QSLC_ECUDA, "upload failed");
     if (!rc && cudaMemcpy(b->d_order, b->order.data(), ninst * 4, cudaMemcpyHostToDevice) != cudaSuccess)
         rc = fail(QSLC_ECUDA, "upload failed");
-    if (!rc) rc = dtype == QSLC_C128 ? capture<double>(b) : capture<float>(b);
+    if (!rc) {
+        const auto c = candidates(b);
+        if (c.empty()) rc = fail(QSLC_EINVAL, "no launch shape fits the largest instance");
+        else rc = capture_any(b, c.back());    // 1024 threads, one CTA per SM
+    }
     if (rc) {
         batch_free(b);
         return rc;
@@ -358,8 +590,72 @@ extern "C" int qslc_batch_run(qslc_batch *b, const double *angles, const double 
 {
     if (!b || !angles || !probs || (!uniforms && b->nshots) || (!shots && b->nshots))
         return fail(QSLC_EINVAL, "null pointer");
-    return b->dtype == QSLC_C128 ? run_t<double>(b, angles, uniforms, probs, shots)
-                                 : run_t<float>(b, angles, uniforms, probs, shots);
+    std::vector<uint32_t> perm;
+    int rc = upload_any(b, angles, uniforms, perm);
+    if (rc) return rc;
+    QSLC_CUDA(cudaGraphLaunch(b->exec, b->stream));
+    rc = b->dtype == QSLC_C128 ? download<double>(b, perm, probs, shots) : download<float>(b, perm, probs, shots);
+    if (!rc) b->runs++;
+    return rc;
+}
+
+extern "C" int qslc_batch_autotune(qslc_batch *b, const double *angles, const double *uniforms,
+                                   double *best_ms)
+{
+    if (!b || !angles || (!uniforms && b->nshots)) return fail(QSLC_EINVAL, "null pointer");
+    std::vector<uint32_t> perm;
+    int rc = upload_any(b, angles, uniforms, perm);
+    if (rc) return rc;
+    cudaEvent_t e0, e1;
+    QSLC_CUDA(cudaEventCreate(&e0));
+    QSLC_CUDA(cudaEventCreate(&e1));
+    BatchShape best = b->shape;
+    float best_t = -1.f;
+    for (const BatchShape &s : candidates(b)) {
+        rc = capture_any(b, s);
+        if (rc) break;
+        QSLC_CUDA(cudaGraphLaunch(b->exec, b->stream));        // warm-up
+        QSLC_CUDA(cudaEventRecord(e0, b->stream));
+        QSLC_CUDA(cudaGraphLaunch(b->exec, b->stream));
+        QSLC_CUDA(cudaEventRecord(e1, b->stream));
+        QSLC_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        QSLC_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (best_t < 0.f || ms < best_t) {
+            best_t = ms;
+            best = s;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (!rc) rc = capture_any(b, best);
+    if (!rc && best_ms) *best_ms = double(best_t);
+    return rc;
+}
+
+extern "C" int qslc_batch_set_shape(qslc_batch *b, unsigned threads, unsigned tile_log2,
+                                    unsigned ctas_per_sm)
+{
+    if (!b) return fail(QSLC_EINVAL, "null batch");
+    BatchShape s;
+    s.threads = threads;
+    s.tile_log2 = tile_log2;
+    s.ctas_per_sm = ctas_per_sm;
+    for (const BatchShape &c : candidates(b))
+        if (c.threads == s.threads && c.tile_log2 == s.tile_log2 && c.ctas_per_sm == s.ctas_per_sm)
+            return capture_any(b, s);
+    return fail(QSLC_EINVAL, "not one of the launch shapes this batch can take");
+}
+
+extern "C" int qslc_batch_shape(const qslc_batch *b, unsigned *threads, unsigned *tile_log2,
+                                unsigned *ctas_per_sm, unsigned *grid)
+{
+    if (!b) return fail(QSLC_EINVAL, "null batch");
+    if (threads) *threads = b->shape.threads;
+    if (tile_log2) *tile_log2 = b->shape.tile_log2;
+    if (ctas_per_sm) *ctas_per_sm = b->shape.ctas_per_sm;
+    if (grid) *grid = b->grid;
+    return QSLC_OK;
 }
 
 extern "C" int qslc_batch_destroy(qslc_batch *b)

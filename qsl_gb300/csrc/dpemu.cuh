@@ -87,11 +87,10 @@ struct MulConst {
     uint32_t m0, m1; // m split into its low 32 and high 21 bits
 };
 
-inline MulConst make_const(double c)
+QSLC_HD MulConst make_const(double c)
 {
     MulConst k{};
-    uint64_t b;
-    std::memcpy(&b, &c, 8);
+    const uint64_t b = dbits(c);
     const int ef = int((b >> 52) & 0x7FF);
     k.sign = b & SIGN;
     k.usable = (ef != 0 && ef != 0x7FF) ? 1 : 0;

@@ -93,6 +93,62 @@ if (ok) return emu::dfrom(r);
     return NEG ? R::sub(R::mul(a, k1), R::mul(b, k2)) : R::add(R::mul(a, k1), R::mul(b, k2));
 }
 
+enum PairOp { P_SWAP, P_Y, P_H, P_RX, P_RY, P_RZ };
+enum DiagOp { D_NEG, D_PHASE };
+
+// em: bit i set = output i (r0.x, r0.y, r1.x, r1.y) on the integer pipes;
+// it must be the same across a warp.
+template <class T, int OP>
+__device__ __forceinline__ void pair_update(cplx<T> &a0, cplx<T> &a1, const Coef<T> &k, unsigned em = 0)
+{
+    using R = rn<T>;
+    cplx<T> r0, r1;
+    const bool E0 = em & 1, E1 = em & 2, E2 = em & 4, E3 = em & 8;
+    if constexpr (OP == P_SWAP) {            // gates.cpp:41, :236, :524
+        r0 = a1;
+        r1 = a0;
+    } else if constexpr (OP == P_Y) {        // gates.cpp:59-62, :267-270
+        r0.x = a1.y; r0.y = -a1.x;
+        r1.x = -a0.y; r1.y = a0.x;
+    } else if constexpr (OP == P_H) {        // gates.cpp:95-98, :493-496, :675-678
+        r0.x = hdiv<T, false>(E0, a0.x, a1.x, k);
+        r0.y = hdiv<T, false>(E1, a0.y, a1.y, k);
+        r1.x = hdiv<T, true>(E2, a0.x, a1.x, k);
+        r1.y = hdiv<T, true>(E3, a0.y, a1.y, k);
+    } else if constexpr (OP == P_RX) {       // gates.cpp:139-144, :336-341, :595-600
+        r0.x = dot2<T, false>(E0, a0.x, k.c, k.kc, a1.y, k.s, k.ks);
+        r0.y = dot2<T, true>(E1, a0.y, k.c, k.kc, a1.x, k.s, k.ks);
+        r1.x = dot2<T, false>(E2, a1.x, k.c, k.kc, a0.y, k.s, k.ks);
+        r1.y = dot2<T, true>(E3, a1.y, k.c, k.kc, a0.x, k.s, k.ks);
+    } else if constexpr (OP == P_RY) {       // gates.cpp:169-174, :380-385, :638-643
+        r0.x = dot2<T, true>(E0, a0.x, k.c, k.kc, a1.x, k.s, k.ks);
+        r0.y = dot2<T, true>(E1, a0.y, k.c, k.kc, a1.y, k.s, k.ks);
+        r1.x = dot2<T, false>(E2, a0.x, k.s, k.ks, a1.x, k.c, k.kc);
+        r1.y = dot2<T, false>(E3, a0.y, k.s, k.ks, a1.y, k.c, k.kc);
+    } else {                                 // P_RZ: gates.cpp:200-205, :424-429
+        r0.x = dot2<T, false>(E0, a0.x, k.c, k.kc, a0.y, k.s, k.ks);
+        r0.y = dot2<T, true>(E1, a0.y, k.c, k.kc, a0.x, k.s, k.ks);
+        r1.x = dot2<T, true>(E2, a1.x, k.c, k.kc, a1.y, k.s, k.ks);
+        r1.y = dot2<T, false>(E3, a1.y, k.c, k.kc, a1.x, k.s, k.ks);
+    }
+    a0 = r0;
+    a1 = r1;
+}
+
+template <class T, int OP>
+__device__ __forceinline__ void diag_update(cplx<T> &a, const Coef<T> &k, unsigned em = 0)
+{
+    using R = rn<T>;
+    if constexpr (OP == D_NEG) {             // gates.cpp:76-77, :296-297 (x *= -1)
+        a.x = R::mul(a.x, T(-1));
+        a.y = R::mul(a.y, T(-1));
+    } else {                                 // gates.cpp:114-115, :460-461
+        T x = a.x, y = a.y;
+        a.x = dot2<T, true>((em & 1) != 0, x, k.c, k.kc, y, k.s, k.ks);
+        a.y = dot2<T, false>((em & 2) != 0, y, k.c, k.kc, x, k.s, k.ks);
+    }
+}
+
 // The sweeps below take ITEMS work items per grid-stride iteration (at j,
 // j + stride, j + 2 stride), all loads first.  `pat` holds one emulation
 // mask per item, 4 bits each: item r uses (pat >> 4r) & 15, so the share of

@@ -46,3 +46,53 @@ def test_batch_matches_oracle(qsl, port, dtype):
             at += cnt
             assert np.array_equal(probs[i], p), (rep, i, n)
             assert np.array_equal(shots[i], sh), (rep, i, n)
+
+
+@pytest.mark.parametrize("dtype", [np.complex128, np.complex64])
+def test_every_launch_shape_matches_oracle(qsl, port, dtype):
+    """Each launch shape the autotuner can choose -- shared-memory tiles of
+    64 or 128 KB, 512 or 1024 threads, one or two CTAs per SM -- gives the
+    oracle's bits, including instances of twice the tile's qubits (the
+    two-pass path keeping no low qubits whole) and instances that fit a
+    tile exactly."""
+    import os
+    rng = np.random.default_rng(21)
+    fp32 = dtype == np.complex64
+    k = 14 if fp32 else 13
+    ns = np.array([2 * (k - 1), 18, k + 1, k, k - 1, 9, 2], dtype=np.uint32)
+    ls = np.array([1, 2, 2, 2, 1, 3, 2], dtype=np.uint32)
+    nshots = 300
+    b = qsl.Batch(ns, ls, nshots, dtype=dtype)
+    angles = rng.uniform(0, 2 * np.pi, b.angle_count)
+    u = rng.random(ns.size * nshots)
+    if fp32:
+        angles = angles.astype(np.float32).astype(np.float64)
+        u = u.astype(np.float32).astype(np.float64)
+    want, at = [], 0
+    for i, (n, L) in enumerate(zip(ns, ls)):
+        cnt = 2 * int(n) * int(L)
+        sim = port.PortQubits(int(n), fp32=fp32, nthreads=os.cpu_count() or 1)
+        a = angles[at:at + cnt].reshape(int(L), int(n), 2)
+        for l in range(int(L)):
+            for q in range(int(n)):
+                sim.gate("rotateY", q, None, a[l, q, 0])
+            for q in range(int(n)):
+                sim.gate("rotateZ", q, None, a[l, q, 1])
+            for q in range(int(n) - 1):
+                sim.gate("controlNot", q, q + 1)
+        want.append((np.array([[sim.prob(q, 0), sim.prob(q, 1)] for q in range(int(n))]),
+                     sim.sample_all(u[i * nshots:(i + 1) * nshots])))
+        at += cnt
+    shapes = b.shapes()
+    assert len(shapes) >= 3
+    for th, tl, c in shapes:
+        b.set_shape(th, tl, c)
+        assert b.shape()["tile_log2"] == tl
+        probs, shots = b.run(angles, u)
+        for i in range(ns.size):
+            assert np.array_equal(probs[i], want[i][0]), (th, tl, c, i)
+            assert np.array_equal(shots[i], want[i][1]), (th, tl, c, i)
+    ms = b.autotune(angles, u)
+    assert ms > 0 and tuple(b.shape()[x] for x in ("threads", "tile_log2", "ctas_per_sm")) in shapes
+    probs, shots = b.run(angles, u)
+    assert all(np.array_equal(probs[i], want[i][0]) for i in range(ns.size))
