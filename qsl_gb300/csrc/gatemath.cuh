@@ -155,7 +155,18 @@ __device__ __forceinline__ void diag_update(cplx<T> &a, const Coef<T> &k, unsign
 // outputs computed on the integer pipes can be set in steps of one output
 // in twelve (pair gates) or one in six (diagonal gates).  Masks differ only
 // between items, never between threads of a warp.
-constexpr int ITEMS = 3;
+#ifndef QSLC_ITEMS
+#define QSLC_ITEMS 3
+#endif
+constexpr int ITEMS = QSLC_ITEMS;
+
+// Launch bounds of the sweep kernels: 256 threads, and with QSLC_MINB set,
+// at least that many resident CTAs per SM (which caps the registers).
+#if defined(QSLC_MINB) && QSLC_MINB > 0
+#define QSLC_SWEEP_BOUNDS __launch_bounds__(256, QSLC_MINB)
+#else
+#define QSLC_SWEEP_BOUNDS __launch_bounds__(256)
+#endif
 
 // A kernel's pattern is a template argument when it is one of the few
 // compiled in (the mask tests then fold away, and so do the unused
@@ -225,9 +236,9 @@ inline unsigned parse_pattern(const char *var, const char *dflt, unsigned width_
 {
     const char *e = std::getenv(var);
     const char *src = e ? e : dflt;
-    unsigned m[ITEMS] = {0, 0, 0};
+    unsigned m[3] = {0, 0, 0};   // three masks whatever ITEMS is; kernels use the first ITEMS
     int n = 0;
-    for (const char *c = src; *c && n < ITEMS;) {
+    for (const char *c = src; *c && n < 3;) {
         char *endp = nullptr;
         const long v = std::strtol(c, &endp, 10);
         if (endp == c) break;
@@ -235,9 +246,9 @@ inline unsigned parse_pattern(const char *var, const char *dflt, unsigned width_
         c = (*endp == ',') ? endp + 1 : endp;
         if (*endp != ',') break;
     }
-    for (int i = n; i < ITEMS; i++) m[i] = n ? m[n - 1] : 0;
+    for (int i = n; i < 3; i++) m[i] = n ? m[n - 1] : 0;
     unsigned pat = 0;
-    for (int i = 0; i < ITEMS; i++) pat |= m[i] << (4 * i);
+    for (int i = 0; i < 3; i++) pat |= m[i] << (4 * i);
     return pat;
 }
 inline unsigned pattern_rot()

@@ -23,7 +23,7 @@ namespace {
 
 // One-qubit pair gates: pairs (i0, i0 + 2^t), i0 = insert0(j, t).
 template <class T, int OP, unsigned CPAT = PAT_RUNTIME>
-__global__ void __launch_bounds__(256) k_pair1(cplx<T> *__restrict__ st, uint64_t npairs,
+__global__ void QSLC_SWEEP_BOUNDS k_pair1(cplx<T> *__restrict__ st, uint64_t npairs,
                                                unsigned t, Coef<T> k, unsigned pat)
 {
     const uint64_t bit = uint64_t(1) << t;
@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(256) k_pair1(cplx<T> *__restrict__ st, uint64_
 
 // One-qubit diagonal gates on the |1> half: index insert0(j, t) | 2^t.
 template <class T, int OP, unsigned CPAT = PAT_RUNTIME>
-__global__ void __launch_bounds__(256) k_diag1(cplx<T> *__restrict__ st, uint64_t count,
+__global__ void QSLC_SWEEP_BOUNDS k_diag1(cplx<T> *__restrict__ st, uint64_t count,
                                                unsigned t, Coef<T> k, unsigned pat)
 {
     const uint64_t bit = uint64_t(1) << t;
@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(256) k_diag1(cplx<T> *__restrict__ st, uint64_
 // MODE 1: number-preserving pair (base|b1, base|b2);
 // MODE 2: fswap = MODE 1 swap plus negation of base|b1|b2.
 template <class T, int OP, int MODE, unsigned CPAT = PAT_RUNTIME>
-__global__ void __launch_bounds__(256) k_pair2(cplx<T> *__restrict__ st, uint64_t nquads,
+__global__ void QSLC_SWEEP_BOUNDS k_pair2(cplx<T> *__restrict__ st, uint64_t nquads,
                                                unsigned lo, unsigned hi, uint64_t b1,
                                                uint64_t b2, Coef<T> k, unsigned pat)
 {
@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(256) k_pair2(cplx<T> *__restrict__ st, uint64_
 
 // controlZ / controlPhase: the |11> quarter (gates.cpp:277-301, :436-465).
 template <class T, int OP, unsigned CPAT = PAT_RUNTIME>
-__global__ void __launch_bounds__(256) k_diag2(cplx<T> *__restrict__ st, uint64_t nquads,
+__global__ void QSLC_SWEEP_BOUNDS k_diag2(cplx<T> *__restrict__ st, uint64_t nquads,
                                                unsigned lo, unsigned hi, uint64_t both,
                                                Coef<T> k, unsigned pat)
 {

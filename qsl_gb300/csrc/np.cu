@@ -111,7 +111,7 @@ enum NPKind {
 // plain sweeps; `pat` chooses per item which of the two outputs run on the
 // integer pipes (gatemath.cuh).
 template <class T, int K, unsigned CPAT = PAT_RUNTIME>
-__global__ void __launch_bounds__(256) k_np_single(cplx<T> *__restrict__ st,
+__global__ void QSLC_SWEEP_BOUNDS k_np_single(cplx<T> *__restrict__ st,
                                                    const uint32_t *__restrict__ tab, uint64_t count,
                                                    const uint32_t *__restrict__ rt, unsigned t1,
                                                    unsigned t2, uint32_t addbits, Coef<T> k,
@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(256) k_np_single(cplx<T> *__restrict__ st,
 
 // Pair updates over table {n-2, w-1} (np/gates.cpp:236-415).
 template <class T, int K, unsigned CPAT = PAT_RUNTIME>
-__global__ void __launch_bounds__(256) k_np_pair(cplx<T> *__restrict__ st,
+__global__ void QSLC_SWEEP_BOUNDS k_np_pair(cplx<T> *__restrict__ st,
                                                  const uint32_t *__restrict__ tab, uint64_t count,
                                                  const uint32_t *__restrict__ rt, unsigned lo,
                                                  unsigned hi, uint32_t b1, uint32_t b2, Coef<T> k,
