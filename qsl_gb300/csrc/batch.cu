@@ -183,6 +183,56 @@ __device__ void finish_instance(const cplx<T> *st, const InstDesc &d, T *__restr
     __syncthreads();
 }
 
+// The measurements of a large instance: the final state passes through
+// shared memory one tile at a time, and every sum walks its terms of the
+// tile in index order, so each keeps the reference's sequential order while
+// reading shared instead of global memory.
+template <class T>
+__device__ void finish_big(const cplx<T> *st, cplx<T> *sm, unsigned k, const InstDesc &d,
+                           T *__restrict__ probs, const double *__restrict__ u,
+                           uint64_t *__restrict__ shots, uint32_t nshots)
+{
+    const uint32_t n = d.n;
+    const uint64_t dim = uint64_t(1) << n, chunk = uint64_t(1) << k;
+    const unsigned tid = threadIdx.x, nt = blockDim.x;
+    const uint32_t q = tid >> 1, o = tid & 1;
+    T p = T(0);
+    double run = 0.0;
+    uint32_t kk = 0;
+    uint64_t *out = shots + d.shots;
+    for (uint64_t c = 0; c < (dim >> k); c++) {
+        __syncthreads();
+        for (uint64_t i = tid; i < chunk; i += nt) sm[i] = st[(c << k) + i];
+        __syncthreads();
+        if (tid < 2 * n) {
+            // prob(q, o): the terms with bit q == o (measure.cpp:126-147)
+            if (q < k) {
+                const uint64_t ob = uint64_t(o) << q;
+                for (uint64_t j = 0; j < (chunk >> 1); j++) {
+                    const cplx<T> a = sm[insert0(j, q) | ob];
+                    p = rn<T>::add(p, norm2_rn(a.x, a.y));
+                }
+            } else if (((c >> (q - k)) & 1) == o) {
+                for (uint64_t i = 0; i < chunk; i++) {
+                    const cplx<T> a = sm[i];
+                    p = rn<T>::add(p, norm2_rn(a.x, a.y));
+                }
+            }
+        } else if (tid == 2 * n) {
+            // the sampling CDF merged against the sorted uniforms
+            for (uint64_t i = 0; i < chunk && kk < nshots; i++) {
+                const cplx<T> a = sm[i];
+                run = __dadd_rn(run, double(norm2_rn(a.x, a.y)));
+                while (kk < nshots && u[kk] <= run) out[kk++] = (c << k) + i;
+            }
+        }
+    }
+    if (tid < 2 * n) probs[d.probs + 2 * q + o] = p;
+    else if (tid == 2 * n)
+        for (; kk < nshots; kk++) out[kk] = 0;       // above the total: index 0
+    __syncthreads();
+}
+
 // An instance that fits one tile: the whole circuit in shared memory.
 template <class T>
 __device__ void run_small(cplx<T> *sm, LayerCoefs<T> &lc, const InstDesc &d, const T *coef)
@@ -303,8 +353,7 @@ __global__ void __launch_bounds__(1024) k_batch(BatchArgs a)
             finish_instance<T>(sm, d, probs, u, a.shots, a.nshots);
         } else {
             const cplx<T> *fin = run_big<T>(sm, lc, d, coef, slot, slot + a.slot_amps, a.tile_log2);
-            __syncthreads();
-            finish_instance<T>(fin, d, probs, u, a.shots, a.nshots);
+            finish_big<T>(fin, sm, a.tile_log2, d, probs, u, a.shots, a.nshots);
         }
     }
 }
