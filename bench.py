@@ -345,16 +345,12 @@ def run_gpu(args):
     import torch
     import qsl_gb300 as q
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    from qsl_gb300.replicas import Replicas
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    rep = Replicas("nccl")          # one independent replica per GPU; no data-path collective
+    rank, world = rep.rank, rep.world
     n = args.qubits
-    circ = workloads.layered_mixed(n, LAYERS, SEED + rank)
+    circ = workloads.layered_mixed(n, LAYERS, rep.seed(SEED))
     layers = layers_of(circ, n)
     stream = torch.cuda.Stream()
     sim = q.Qubits(n)
@@ -376,8 +372,7 @@ def run_gpu(args):
         run_layer(w, None)
     sim.synchronize()
     torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
+    rep.barrier()
 
     clocks = ClockSampler()
     clocks.start()
@@ -393,12 +388,11 @@ def run_gpu(args):
     torch.cuda.synchronize()
     launches = sim.launches() - launches0
     clk = clocks.stop()
-    total_ms = t_start.elapsed_time(t_end)
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    rep.barrier()
+    local_ms = t_start.elapsed_time(t_end)
     ngates = sum(len(layers[(args.warmup + k) % len(layers)]) for k in range(args.steps))
+    total_ms = rep.max(local_ms)                      # the slowest rank
+    job_gates_per_s = rep.throughput(ngates, local_ms * 1e-3)
 
     # per-kernel breakdown from the per-gate events
     per = {}
@@ -453,7 +447,7 @@ def run_gpu(args):
         del sim2, host
 
     line = {
-        "metric": METRIC, "value": ngates / (total_ms * 1e-3) * world, "unit": UNIT,
+        "metric": METRIC, "value": job_gates_per_s, "unit": UNIT,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -498,10 +492,8 @@ def run_gpu(args):
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": thr, "kind": "port",
                                 "sample": f"first {done} gates of the same {n}-qubit circuit, "
                                           f"OpenMP restatement of the reference's Omp backend"}
-    if dist:
-        dist.barrier()
-        dist.destroy_process_group()
-    if rank == 0:
+    rep.close()
+    if rep.leader:
         print(json.dumps(line), flush=True)
 
 
