@@ -277,7 +277,7 @@ inline unsigned pattern_np_pair()
 }
 inline unsigned pattern_np_diag()
 {
-    static unsigned p = parse_pattern("QSLC_EMU_MASK_NP_DIAG", "1,0,0", 3);
+    static unsigned p = parse_pattern("QSLC_EMU_MASK_NP_DIAG", "1,1,0", 3);
     return p;
 }
 
