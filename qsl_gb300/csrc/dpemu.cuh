@@ -85,6 +85,9 @@ struct MulConst {
     uint64_t sign;   // SIGN or 0
     int usable;      // 0: zero/subnormal/inf/nan -- always use the native path
     uint32_t m0, m1; // m split into its low 32 and high 21 bits
+    // biased exponents ef of a normal multiplicand for which a * c and its
+    // rounding stay normal: ef - ef_lo <= ef_span (unsigned), one test
+    uint32_t ef_lo, ef_span;
 };
 
 QSLC_HD MulConst make_const(double c)
@@ -98,6 +101,13 @@ QSLC_HD MulConst make_const(double c)
     k.e = ef - 1023;
     k.m0 = uint32_t(k.m);
     k.m1 = uint32_t(k.m >> 32);
+    // product exponent ef - 1023 + e (+1 for a carry, +1 for a rounding
+    // overflow) must stay in [-1022, 1023]
+    const int lo = 1 - k.e > 1 ? 1 - k.e : 1;
+    const int hi = 2044 - k.e < 2046 ? 2044 - k.e : 2046;
+    if (lo > hi) k.usable = 0;
+    k.ef_lo = uint32_t(lo);
+    k.ef_span = lo > hi ? 0u : uint32_t(hi - lo);
     return k;
 }
 
@@ -197,6 +207,10 @@ struct DivConst {
     int e;           // unbiased exponent
     uint64_t sign;
     int usable;
+    uint64_t half;   // m >> 1: the remainder above it rounds up
+    uint64_t tie;    // 1 when m is even (only then can a remainder equal m / 2)
+    // biased exponents of a normal dividend whose quotient stays normal
+    uint32_t ef_lo, ef_span;
 };
 
 inline DivConst make_div(double y)
@@ -211,7 +225,49 @@ inline DivConst make_div(double y)
     k.e = ef - 1023;
     const unsigned __int128 num = ((unsigned __int128)1 << 116) - 1;
     k.rinv = (uint64_t)(num / k.m);
+    k.half = k.m >> 1;
+    k.tie = (k.m & 1) ? 0 : 1;
+    // quotient exponent ef - 1023 - e - (0 or 1) must stay in [-1021, 1022]
+    const int lo = 3 + k.e > 1 ? 3 + k.e : 1;
+    const int hi = 2045 + k.e < 2046 ? 2045 + k.e : 2046;
+    if (lo > hi) k.usable = 0;
+    k.ef_lo = uint32_t(lo);
+    k.ef_span = lo > hi ? 0u : uint32_t(hi - lo);
     return k;
+}
+
+// RN(x / y), x packed, y a normal constant: the hot form of the division.
+// The quotient significand t = floor(mx * 2^k / my) (k = 52 or 53, so
+// that t has 53 bits) comes from the high part of the full product of mx
+// and the 64-bit reciprocal, which is low by at most one; the exact
+// remainder corrects it once and, against my / 2, rounds it.  The rounding
+// increment goes into the packed result, so a carry moves into the
+// exponent by itself.
+QSLC_HD uint64_t div_fast(uint64_t x, const DivConst &y, bool &ok)
+{
+    const uint32_t xhi = uint32_t(x >> 32), xlo = uint32_t(x);
+    const uint32_t ef = (xhi >> 20) & 0x7FF;
+    const uint32_t sg = (xhi ^ uint32_t(y.sign >> 32)) & 0x80000000u;
+    if (((xhi << 1) | xlo) == 0) return uint64_t(sg) << 32;     // +-0 / y
+    ok = ok & ((ef - y.ef_lo) <= y.ef_span);
+    const uint32_t m1 = (xhi & 0xFFFFFu) | 0x100000u, m0 = xlo;
+    const uint64_t mx = (uint64_t(m1) << 32) | m0;
+    const uint32_t r0 = uint32_t(y.rinv), r1 = uint32_t(y.rinv >> 32);
+    const uint64_t a = uint64_t(m0) * r1, b = uint64_t(m1) * r0;
+    const uint64_t h = (uint64_t(m0) * r0) >> 32;
+    const uint64_t s1 = a + b;
+    const uint64_t s2 = s1 + h;
+    const uint64_t carry = uint64_t(s1 < a) + uint64_t(s2 < s1);
+    const uint64_t hi = uint64_t(m1) * r1 + (s2 >> 32) + (carry << 32);   // product >> 64
+    const uint64_t k53 = uint64_t(mx < y.m);
+    uint64_t t = (hi << k53) | ((s2 >> 31) & k53);            // bit 63 of the product is bit 31 of s2
+    uint64_t r = (mx << (52 + k53)) - t * y.m;
+    const bool c = r >= y.m;
+    t += c ? 1 : 0;
+    r -= c ? y.m : 0;
+    const uint64_t inc = uint64_t(r > y.half) | (uint64_t(r == y.half) & y.tie & (t & 1));
+    const int E = int(ef) - 1023 - y.e - int(k53);
+    return (uint64_t(sg) << 32) | ((uint64_t(uint32_t(E + 1022)) << 52) + t + inc);
 }
 
 // RN(x / y) for a normal constant y.  The quotient significand
@@ -419,13 +475,80 @@ QSLC_HD uint64_t div_unp(const Unp &x, const DivConst &y, bool &ok)
 // every rotation and phase output in qsl's gate loops (e.g. a0.real*cos +
 // a1.imag*sin, gates.cpp:139).  `ok` reports whether the integer path
 // covered every step; when it did not, the result is meaningless.
+//
+// The code below is the hot form, written for 32-bit integer pipes:
+//  - a product is RN(a * c) with its significand left unnormalised when the
+//    rounding carries out (m = 2^53 then stands for 2^52 at exponent + 1),
+//    and a zero product is m = 0 with an exponent far below any other;
+//  - the sum orders its operands by exponent only.  With equal exponents a
+//    subtraction may come out negative; it is then negated, which is exact
+//    because no bits were shifted out;
+//  - it normalises by a single left shift by the count of leading zeros,
+//    which also covers the carry of an addition;
+//  - the rounding increment is added to the packed result, so a carry out
+//    of the significand moves into the exponent field by itself.
+// Operands outside the normal range (or whose products or sum would leave
+// it) set ok = false.
+
+// RN(a * c): significand (53 bits, or 2^53), exponent, sign in bit 31.
+QSLC_HD void prod_fast(uint64_t a, const MulConst &c, uint64_t &m, int &e, uint32_t &sg, bool &ok)
+{
+    const uint32_t ahi = uint32_t(a >> 32), alo = uint32_t(a);
+    const uint32_t ef = (ahi >> 20) & 0x7FF;
+    sg = (ahi ^ uint32_t(c.sign >> 32)) & 0x80000000u;
+    const bool zero = ((ahi << 1) | alo) == 0;
+    ok = ok & (zero | ((ef - c.ef_lo) <= c.ef_span));
+    const uint32_t a1 = (ahi & 0xFFFFFu) | 0x100000u;
+    const uint64_t p00 = uint64_t(alo) * c.m0, p01 = uint64_t(alo) * c.m1;
+    const uint64_t p10 = uint64_t(a1) * c.m0, p11 = uint64_t(a1) * c.m1;
+    const uint64_t mid = p01 + p10;
+    const uint64_t lo = p00 + (mid << 32);
+    const uint64_t hi = p11 + (mid >> 32) + uint64_t(lo < p00);   // product = hi:lo < 2^106
+    const uint32_t top = uint32_t(hi >> 41);
+    uint64_t q = (hi << 13) | (lo >> 51);                          // product >> 51
+    uint64_t st = uint64_t((lo & ((uint64_t(1) << 51) - 1)) != 0);
+    st |= q & top;
+    q >>= top;
+    uint64_t mm = q >> 1;
+    mm += (q & 1) & (st | (mm & 1));
+    m = zero ? 0 : mm;
+    e = zero ? -4000 : int(ef) - 1023 + c.e + int(top);
+}
+
 QSLC_HD uint64_t dot2_rn(uint64_t a, const MulConst &c, uint64_t b, const MulConst &s, bool neg,
                          bool &ok)
 {
-    const Unp p = mul_unp(a, c, ok);
-    Unp q = mul_unp(b, s, ok);
-    if (neg) q.sign ^= SIGN;
-    return add_unp(p, q, ok);
+    uint64_t mp, mq;
+    int ep, eq;
+    uint32_t sp, sq;
+    prod_fast(a, c, mp, ep, sp, ok);
+    prod_fast(b, s, mq, eq, sq, ok);
+    if (neg) sq ^= 0x80000000u;
+    // x: the operand with the larger exponent
+    const bool sw = eq > ep;
+    const uint64_t mx = sw ? mq : mp, my = sw ? mp : mq;
+    const int ex = sw ? eq : ep, ey = sw ? ep : eq;
+    const uint32_t sx = sw ? sq : sp, sy = sw ? sp : sq;
+    const uint64_t X = mx << 9, Yf = my << 9;       // lead bit at 61 (62 for 2^53)
+    const unsigned dd = unsigned(ex - ey);
+    const unsigned d = dd > 63 ? 63 : dd;
+    const uint64_t Y = (Yf >> d) | uint64_t((Yf & ((uint64_t(1) << d) - 1)) != 0);
+    const bool sub = (sx ^ sy) != 0;
+    int64_t S = int64_t(sub ? X - Y : X + Y);
+    uint32_t rs = sx;
+    if (S < 0) {                                    // equal exponents, |y| > |x|
+        S = -S;
+        rs ^= 0x80000000u;
+    }
+    if (S == 0) return uint64_t(sub ? 0u : (sx & sy)) << 32;
+    const int lz = clz64(uint64_t(S));              // >= 1
+    const uint64_t N = uint64_t(S) << lz;           // lead bit at 63
+    const int E = ex + 2 - lz;
+    const uint64_t mr = N >> 11;
+    const uint64_t rb = N & 0x7FF;
+    const uint64_t inc = uint64_t(rb > 0x400) | (uint64_t(rb == 0x400) & (mr & 1));
+    ok = ok & (E >= -1021) & (E <= 1022);
+    return (uint64_t(rs) << 32) | ((uint64_t(uint32_t(E + 1022)) << 52) + mr + inc);
 }
 
 }  // namespace emu

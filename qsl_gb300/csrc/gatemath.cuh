@@ -55,16 +55,15 @@ __device__ __forceinline__ T hdiv(bool em, T a, T b, const Coef<T> &k)
     if constexpr (sizeof(T) == 8) {
         bool ok = k.kd.usable != 0;
         if (ok) {
-            emu::Unp sum;
+            uint64_t q;
             if (em) {
                 const emu::Unp x = emu::unpack(emu::dbits(a), ok);
                 emu::Unp y = emu::unpack(emu::dbits(b), ok);
                 if (NEG) y.sign ^= emu::SIGN;
-                sum = emu::add_core(x, y, ok);
+                q = emu::div_unp(emu::add_core(x, y, ok), k.kd, ok);
             } else {
-                sum = emu::unpack(emu::dbits(NEG ? R::sub(a, b) : R::add(a, b)), ok);
+                q = emu::div_fast(emu::dbits(NEG ? R::sub(a, b) : R::add(a, b)), k.kd, ok);
             }
-            const uint64_t q = emu::div_unp(sum, k.kd, ok);
             if (ok) return emu::dfrom(q);
         }
         return hdiv_fallback<NEG>(a, b, k.c);

@@ -8,6 +8,7 @@
 
 #include <cstdio>
 #include <cstdlib>
+#include <cmath>
 #include <random>
 
 using namespace qslc::emu;
@@ -77,6 +78,16 @@ int main(int argc, char **argv)
             if (ok && qd != dbits(qref)) {
                 if (fails++ < 10) std::printf("div %a / %a: got %a want %a\n", xv, yv, dfrom(qd), (double)qref);
             }
+            // the hot form of the division
+            {
+                bool ok5 = kd.usable != 0;
+                const uint64_t qf = div_fast(dbits(xv), kd, ok5);
+                if (ok5 && qf != dbits(qref)) {
+                    if (fails++ < 10)
+                        std::printf("div_fast %a / %a: got %a want %a\n", xv, yv, dfrom(qf), (double)qref);
+                }
+                if (!ok5) declined_div++;
+            }
             // the unpacked division must agree with the packed one bit for bit
             {
                 bool ok2 = kd.usable != 0;
@@ -114,6 +125,12 @@ int main(int argc, char **argv)
             if (ok && qd != dbits(qref2)) {
                 if (fails++ < 10) std::printf("div2 %a / %a: got %a want %a\n", prod, yv, dfrom(qd), (double)qref2);
             }
+            bool ok6 = kd.usable != 0;
+            const uint64_t qf2 = div_fast(dbits(prod), kd, ok6);
+            if (ok6 && qf2 != dbits(qref2)) {
+                if (fails++ < 10)
+                    std::printf("div_fast2 %a / %a: got %a want %a\n", prod, yv, dfrom(qf2), (double)qref2);
+            }
             bool ok4 = kd.usable != 0;
             const uint64_t qu2 = div_unp(unpack(dbits(prod), ok4), kd, ok4);
             if (ok4 && qu2 != dbits(qref2)) {
@@ -146,6 +163,21 @@ int main(int argc, char **argv)
                                 dfrom(d), (double)dref);
             }
             if (!ok) declined_dot++;
+        }
+    }
+    // exact halfway quotients for divisors with an even significand:
+    // x = y * (k + 1/2), so x / y rounds to the even neighbour of k + 1/2
+    for (long i = 0; i < N / 20; i++) {
+        const double ys[4] = {1.5, 1.25, 1.75, 1.125};
+        const double yv = ys[i & 3];
+        const uint64_t k = (rng() >> 17) | 1;                          // < 2^47: y * (k + 1/2) is exact
+        const double xv = std::ldexp(yv * (double(k) + 0.5), int(rng() % 40) - 20);
+        DivConst kd = make_div(yv);
+        bool okh = true;
+        const uint64_t q = div_fast(dbits(xv), kd, okh);
+        volatile double qref = xv / yv;
+        if (okh && q != dbits(qref)) {
+            if (fails++ < 10) std::printf("div tie %a / %a: got %a want %a\n", xv, yv, dfrom(q), (double)qref);
         }
     }
     std::printf("cases %ld fails %ld declined mul %ld add %ld dot2 %ld\n", N, fails, declined_mul,
