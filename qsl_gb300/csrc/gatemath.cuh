@@ -148,6 +148,20 @@ __device__ __forceinline__ void diag_update(cplx<T> &a, const Coef<T> &k, unsign
     }
 }
 
+// Bit insertion in the index type of a sweep: 32-bit arithmetic for states
+// of up to 31 qubits (every index and shift then fits), 64-bit above.
+template <class IX>
+__host__ __device__ __forceinline__ IX ins0(IX j, unsigned t)
+{
+    const IX low = j & ((IX(1) << t) - 1);
+    return ((j >> t) << (t + 1)) | low;
+}
+template <class IX>
+__host__ __device__ __forceinline__ IX ins00(IX j, unsigned lo, unsigned hi)
+{
+    return ins0<IX>(ins0<IX>(j, lo), hi);
+}
+
 // The sweeps below take ITEMS work items per grid-stride iteration (at j,
 // j + stride, j + 2 stride), all loads first.  `pat` holds one emulation
 // mask per item, 4 bits each: item r uses (pat >> 4r) & 15, so the share of

@@ -22,19 +22,19 @@ namespace {
 
 
 // One-qubit pair gates: pairs (i0, i0 + 2^t), i0 = insert0(j, t).
-template <class T, int OP, unsigned CPAT = PAT_RUNTIME>
+template <class T, int OP, unsigned CPAT = PAT_RUNTIME, class IX = uint64_t>
 __global__ void QSLC_SWEEP_BOUNDS k_pair1(cplx<T> *__restrict__ st, uint64_t npairs,
                                                unsigned t, Coef<T> k, unsigned pat)
 {
-    const uint64_t bit = uint64_t(1) << t;
-    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    const IX bit = IX(1) << t;
+    const IX stride = IX(gridDim.x) * blockDim.x;
     const unsigned pt = CPAT == PAT_RUNTIME ? pat : CPAT;
-    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < npairs; j += ITEMS * stride) {
+    for (IX j = IX(blockIdx.x) * blockDim.x + threadIdx.x; j < IX(npairs); j += ITEMS * stride) {
         cplx<T> a0[ITEMS], a1[ITEMS];
-        uint64_t i0[ITEMS];
+        IX i0[ITEMS];
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
-            i0[r] = insert0(j + r * stride, t);
+            i0[r] = ins0<IX>(j + r * stride, t);
             if (j + r * stride < npairs) {
                 a0[r] = st[i0[r]];
                 a1[r] = st[i0[r] | bit];
@@ -52,19 +52,19 @@ __global__ void QSLC_SWEEP_BOUNDS k_pair1(cplx<T> *__restrict__ st, uint64_t npa
 }
 
 // One-qubit diagonal gates on the |1> half: index insert0(j, t) | 2^t.
-template <class T, int OP, unsigned CPAT = PAT_RUNTIME>
+template <class T, int OP, unsigned CPAT = PAT_RUNTIME, class IX = uint64_t>
 __global__ void QSLC_SWEEP_BOUNDS k_diag1(cplx<T> *__restrict__ st, uint64_t count,
                                                unsigned t, Coef<T> k, unsigned pat)
 {
-    const uint64_t bit = uint64_t(1) << t;
-    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    const IX bit = IX(1) << t;
+    const IX stride = IX(gridDim.x) * blockDim.x;
     const unsigned pt = CPAT == PAT_RUNTIME ? pat : CPAT;
-    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < count; j += ITEMS * stride) {
+    for (IX j = IX(blockIdx.x) * blockDim.x + threadIdx.x; j < IX(count); j += ITEMS * stride) {
         cplx<T> a[ITEMS];
-        uint64_t i[ITEMS];
+        IX i[ITEMS];
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
-            i[r] = insert0(j + r * stride, t) | bit;
+            i[r] = ins0<IX>(j + r * stride, t) | bit;
             if (j + r * stride < count) a[r] = st[i[r]];
         }
 #pragma unroll
@@ -84,21 +84,21 @@ __global__ void QSLC_SWEEP_BOUNDS k_diag1(cplx<T> *__restrict__ st, uint64_t cou
 // MODE 0: controlled pair (base|b1, base|b1|b2), b1 = control bit;
 // MODE 1: number-preserving pair (base|b1, base|b2);
 // MODE 2: fswap = MODE 1 swap plus negation of base|b1|b2.
-template <class T, int OP, int MODE, unsigned CPAT = PAT_RUNTIME>
+template <class T, int OP, int MODE, unsigned CPAT = PAT_RUNTIME, class IX = uint64_t>
 __global__ void QSLC_SWEEP_BOUNDS k_pair2(cplx<T> *__restrict__ st, uint64_t nquads,
                                                unsigned lo, unsigned hi, uint64_t b1,
                                                uint64_t b2, Coef<T> k, unsigned pat)
 {
-    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    const IX stride = IX(gridDim.x) * blockDim.x;
     const unsigned pt = CPAT == PAT_RUNTIME ? pat : CPAT;
-    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < nquads; j += ITEMS * stride) {
+    for (IX j = IX(blockIdx.x) * blockDim.x + threadIdx.x; j < IX(nquads); j += ITEMS * stride) {
         cplx<T> a0[ITEMS], a1[ITEMS];
-        uint64_t x1[ITEMS], x2[ITEMS];
+        IX x1[ITEMS], x2[ITEMS];
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
-            const uint64_t base = insert00(j + r * stride, lo, hi);
-            x1[r] = base | b1;
-            x2[r] = (MODE == 0) ? (x1[r] | b2) : (base | b2);
+            const IX base = ins00<IX>(j + r * stride, lo, hi);
+            x1[r] = base | IX(b1);
+            x2[r] = (MODE == 0) ? (x1[r] | IX(b2)) : (base | IX(b2));
             if (j + r * stride < nquads) {
                 a0[r] = st[x1[r]];
                 a1[r] = st[x2[r]];
@@ -111,7 +111,7 @@ __global__ void QSLC_SWEEP_BOUNDS k_pair2(cplx<T> *__restrict__ st, uint64_t nqu
                 st[x1[r]] = a0[r];
                 st[x2[r]] = a1[r];
                 if constexpr (MODE == 2) {
-                    const uint64_t x3 = x1[r] | b2;
+                    const IX x3 = x1[r] | IX(b2);
                     cplx<T> a = st[x3];
                     diag_update<T, D_NEG>(a, k);
                     st[x3] = a;
@@ -122,19 +122,19 @@ __global__ void QSLC_SWEEP_BOUNDS k_pair2(cplx<T> *__restrict__ st, uint64_t nqu
 }
 
 // controlZ / controlPhase: the |11> quarter (gates.cpp:277-301, :436-465).
-template <class T, int OP, unsigned CPAT = PAT_RUNTIME>
+template <class T, int OP, unsigned CPAT = PAT_RUNTIME, class IX = uint64_t>
 __global__ void QSLC_SWEEP_BOUNDS k_diag2(cplx<T> *__restrict__ st, uint64_t nquads,
                                                unsigned lo, unsigned hi, uint64_t both,
                                                Coef<T> k, unsigned pat)
 {
-    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    const IX stride = IX(gridDim.x) * blockDim.x;
     const unsigned pt = CPAT == PAT_RUNTIME ? pat : CPAT;
-    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < nquads; j += ITEMS * stride) {
+    for (IX j = IX(blockIdx.x) * blockDim.x + threadIdx.x; j < IX(nquads); j += ITEMS * stride) {
         cplx<T> a[ITEMS];
-        uint64_t i[ITEMS];
+        IX i[ITEMS];
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
-            i[r] = insert00(j + r * stride, lo, hi) | both;
+            i[r] = ins00<IX>(j + r * stride, lo, hi) | IX(both);
             if (j + r * stride < nquads) a[r] = st[i[r]];
         }
 #pragma unroll
@@ -194,6 +194,15 @@ __global__ void k_set_one(cplx<T> *st, uint64_t pos)
     st[pos] = one;
 }
 
+// Sweeps of states of up to 31 qubits index in 32 bits (fewer integer
+// operations per amplitude); larger states in 64 bits.
+template <class F>
+void with_index(unsigned n, F &&f)
+{
+    if (n <= 31) f(uint32_t(0));
+    else f(uint64_t(0));
+}
+
 template <class T>
 int gate1_t(qslc_state *s, int gate, unsigned t, double angle)
 {
@@ -206,7 +215,9 @@ int gate1_t(qslc_state *s, int gate, unsigned t, double angle)
     auto pair = [&](auto op, unsigned pat, const Coef<T> &k, auto cands) {
         constexpr int OP = decltype(op)::value;
         cands(pat, [&](auto c) {
-            k_pair1<T, OP, decltype(c)::value><<<grid, 256, 0, str>>>(st, half, t, k, pat);
+            with_index(s->n, [&](auto ix) {
+                k_pair1<T, OP, decltype(c)::value, decltype(ix)><<<grid, 256, 0, str>>>(st, half, t, k, pat);
+            });
         });
     };
     auto rot_c = [](unsigned p, auto f) { with_pattern<QSLC_ROT_PATTERNS>(p, f); };
@@ -219,11 +230,17 @@ int gate1_t(qslc_state *s, int gate, unsigned t, double angle)
     case QSLC_ROTATE_X: pair(std::integral_constant<int, P_RX>{}, rot, half_angle<T>(angle), rot_c); break;
     case QSLC_ROTATE_Y: pair(std::integral_constant<int, P_RY>{}, rot, half_angle<T>(angle), rot_c); break;
     case QSLC_ROTATE_Z: pair(std::integral_constant<int, P_RZ>{}, rot, half_angle<T>(angle), rot_c); break;
-    case QSLC_PAULI_Z: k_diag1<T, D_NEG, 0u><<<grid, 256, 0, str>>>(st, half, t, Coef<T>{}, 0); break;
+    case QSLC_PAULI_Z:
+        with_index(s->n, [&](auto ix) {
+            k_diag1<T, D_NEG, 0u, decltype(ix)><<<grid, 256, 0, str>>>(st, half, t, Coef<T>{}, 0);
+        });
+        break;
     case QSLC_PHASE: {
         const Coef<T> k = full_angle<T>(angle);
         with_pattern<QSLC_DIAG_PATTERNS>(dg, [&](auto c) {
-            k_diag1<T, D_PHASE, decltype(c)::value><<<grid, 256, 0, str>>>(st, half, t, k, dg);
+            with_index(s->n, [&](auto ix) {
+                k_diag1<T, D_PHASE, decltype(c)::value, decltype(ix)><<<grid, 256, 0, str>>>(st, half, t, k, dg);
+            });
         });
         break;
     }
@@ -249,7 +266,10 @@ int gate2_t(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle)
     auto pair = [&](auto op, auto mode, unsigned pat, const Coef<T> &k, auto cands) {
         constexpr int OP = decltype(op)::value, MODE = decltype(mode)::value;
         cands(pat, [&](auto c) {
-            k_pair2<T, OP, MODE, decltype(c)::value><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1, b2, k, pat);
+            with_index(s->n, [&](auto ix) {
+                k_pair2<T, OP, MODE, decltype(c)::value, decltype(ix)><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1, b2,
+                                                                                            k, pat);
+            });
         });
     };
     auto rot_c = [](unsigned p, auto f) { with_pattern<QSLC_ROT_PATTERNS>(p, f); };
@@ -281,12 +301,17 @@ int gate2_t(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle)
     case QSLC_NP_HADAMARD: pair(std::integral_constant<int, P_H>{}, M1{}, had, sqrt2_coef<T>(), h_c); break;
     case QSLC_FSWAP: pair(std::integral_constant<int, P_SWAP>{}, M2{}, 0, Coef<T>{}, none); break;
     case QSLC_CONTROL_Z:
-        k_diag2<T, D_NEG, 0u><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1 | b2, Coef<T>{}, 0);
+        with_index(s->n, [&](auto ix) {
+            k_diag2<T, D_NEG, 0u, decltype(ix)><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1 | b2, Coef<T>{}, 0);
+        });
         break;
     case QSLC_CONTROL_PHASE: {
         const Coef<T> k = full_angle<T>(angle);
         with_pattern<QSLC_DIAG_PATTERNS>(dg, [&](auto c) {
-            k_diag2<T, D_PHASE, decltype(c)::value><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1 | b2, k, dg);
+            with_index(s->n, [&](auto ix) {
+                k_diag2<T, D_PHASE, decltype(c)::value, decltype(ix)><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1 | b2,
+                                                                                         k, dg);
+            });
         });
         break;
     }
