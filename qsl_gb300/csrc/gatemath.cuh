@@ -276,7 +276,7 @@ inline unsigned pattern_h()
 }
 inline unsigned pattern_diag()
 {
-    static unsigned p = parse_pattern("QSLC_EMU_MASK_DIAG", "1,1,0", 3);
+    static unsigned p = parse_pattern("QSLC_EMU_MASK_DIAG", "1", 3);
     return p;
 }
 // The number-preserving sweeps spend integer work on ranking their indices,
