@@ -76,9 +76,10 @@ def kernel_of(gate: str) -> str:
 
 # DRAM bytes per launch over algorithmic bytes for the dense one-qubit
 # kernels, from the ncu capture summarised in
-# profiles/k_pair1_dense_gates_26q.md (2.092 GB moved for 2.147 GB of
-# algorithmic traffic at 26 qubits; it scales with the amplitude count).
-K_PAIR1_TRAFFIC_RATIO = 2.092 / 2.147
+# profiles/k_pair1_dense_gates_26q.md (2.086 GB moved for 2.147 GB of
+# algorithmic traffic at 26 qubits on a dense state; it scales with the
+# amplitude count).
+K_PAIR1_TRAFFIC_RATIO = 2.086 / 2.147
 
 
 def peaks():
@@ -471,9 +472,10 @@ def run_gpu(args):
                          if top_name.startswith("k_pair1") else None),
                      "traffic_source": "ncu dram__bytes_read+write of k_pair1 at 26 qubits, "
                                        "scaled by amplitudes (profiles/k_pair1_dense_gates_26q.md)",
-                     "limiter": "FP64 pipe (82% active in ncu): the reference's rounding costs "
-                                "12 FP64 operations per amplitude pair, of which 5 of every 12 "
-                                "outputs run on the integer pipes (exact binary64 emulation)"},
+                     "limiter": "FP64 and integer ALU pipes together (80% and 73% active in "
+                                "ncu on a dense state): the reference's rounding costs 12 FP64 "
+                                "operations per amplitude pair; 5 of every 12 outputs run on the "
+                                "integer pipes instead (exact binary64 emulation)"},
         "gpu_launches": launches,
         "clocks": clk,
     }
