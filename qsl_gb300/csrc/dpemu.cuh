@@ -529,7 +529,11 @@ QSLC_HD uint64_t dot2_rn(uint64_t a, const MulConst &c, uint64_t b, const MulCon
     const uint64_t mx = sw ? mq : mp, my = sw ? mp : mq;
     const int ex = sw ? eq : ep, ey = sw ? ep : eq;
     const uint32_t sx = sw ? sq : sp, sy = sw ? sp : sq;
-    const uint64_t X = mx << 9, Yf = my << 9;       // lead bit at 61 (62 for 2^53)
+    // lead bit at 60 (61 for 2^53), so even the sum of two products that both
+    // rounded up to 2^53 stays below 2^63 and reads as positive; with at
+    // least 8 trailing zeros in both, no bit is dropped unless d > 8, and
+    // then the result keeps its lead within one place of bit 60
+    const uint64_t X = mx << 8, Yf = my << 8;
     const unsigned dd = unsigned(ex - ey);
     const unsigned d = dd > 63 ? 63 : dd;
     const uint64_t Y = (Yf >> d) | uint64_t((Yf & ((uint64_t(1) << d) - 1)) != 0);
@@ -541,9 +545,9 @@ QSLC_HD uint64_t dot2_rn(uint64_t a, const MulConst &c, uint64_t b, const MulCon
         rs ^= 0x80000000u;
     }
     if (S == 0) return uint64_t(sub ? 0u : (sx & sy)) << 32;
-    const int lz = clz64(uint64_t(S));              // >= 1
+    const int lz = clz64(uint64_t(S));              // >= 2
     const uint64_t N = uint64_t(S) << lz;           // lead bit at 63
-    const int E = ex + 2 - lz;
+    const int E = ex + 3 - lz;
     const uint64_t mr = N >> 11;
     const uint64_t rb = N & 0x7FF;
     const uint64_t inc = uint64_t(rb > 0x400) | (uint64_t(rb == 0x400) & (mr & 1));

@@ -28,6 +28,20 @@ static double make(int emin, int emax)
     return dfrom(b);
 }
 
+// A significand ma in [2^52, 2^53) whose product with mc rounds up to the
+// next power of two: ma * mc in [2^105 - 2^51, 2^105) (top = 0) or in
+// [2^106 - 2^52, 2^106) (top = 1).  Not every mc has one.
+static bool carry_significand(uint64_t mc, int top, uint64_t &ma)
+{
+    typedef unsigned __int128 u128;
+    const u128 hi = u128(1) << (105 + top);
+    const u128 lo = hi - (u128(1) << (51 + top));
+    const u128 m = (lo + mc - 1) / mc;
+    if (m < HIDDEN || m >= 2 * HIDDEN || m * mc >= hi) return false;
+    ma = uint64_t(m);
+    return true;
+}
+
 int main(int argc, char **argv)
 {
     const long N = argc > 1 ? std::atol(argv[1]) : 20000000;
@@ -179,6 +193,44 @@ int main(int argc, char **argv)
         if (okh && q != dbits(qref)) {
             if (fails++ < 10) std::printf("div tie %a / %a: got %a want %a\n", xv, yv, dfrom(q), (double)qref);
         }
+    }
+    // products that round up to a power of two (significand 2^53 before
+    // normalisation), summed with a second product of the same exponent: two
+    // such products of one sign make the largest sum the dot product forms
+    long carry_cases = 0;
+    for (long i = 0; i < N / 20; i++) {
+        const double c3 = make(-6, 1), s3 = make(-6, 1);
+        const int top_a = int(rng() & 1), top_b = int(rng() & 1);
+        uint64_t ma, mb;
+        if (!carry_significand(make_const(c3).m, top_a, ma)) continue;
+        const bool both = (rng() % 4) != 0;
+        if (both) {
+            if (!carry_significand(make_const(s3).m, top_b, mb)) continue;
+        } else {
+            mb = (rng() & MANT) | HIDDEN;
+        }
+        const int ec = int((dbits(c3) >> 52) & 0x7FF) - 1023, es = int((dbits(s3) >> 52) & 0x7FF) - 1023;
+        const int ea = int(rng() % 40) - 38;
+        // RN(a*c) = 2^(ea+ec+1+top_a); RN(b*s) lands on the same exponent
+        const int eb = ea + ec + top_a - es - (both ? top_b : 0);
+        const double a3 = std::ldexp(double(ma), ea - 52) * ((rng() & 1) ? -1.0 : 1.0);
+        const double b3 = std::ldexp(double(mb), eb - 52) * ((rng() & 1) ? -1.0 : 1.0);
+        const bool neg = rng() & 1;
+        MulConst kc3 = make_const(c3), ks3 = make_const(s3);
+        bool okc = (kc3.usable & ks3.usable) != 0;
+        const uint64_t d = dot2_rn(dbits(a3), kc3, dbits(b3), ks3, neg, okc);
+        volatile double p1 = a3 * c3, p2 = b3 * s3;
+        volatile double dref = neg ? p1 - p2 : p1 + p2;
+        carry_cases++;
+        if (okc && d != dbits(dref)) {
+            if (fails++ < 10)
+                std::printf("dot2 carry %a*%a %c %a*%a: got %a want %a\n", a3, c3, neg ? '-' : '+', b3, s3,
+                            dfrom(d), (double)dref);
+        }
+    }
+    if (carry_cases < N / 500) {
+        std::printf("only %ld carry cases\n", carry_cases);
+        return 3;
     }
     std::printf("cases %ld fails %ld declined mul %ld add %ld dot2 %ld\n", N, fails, declined_mul,
                 declined_add, declined_dot);
