@@ -106,6 +106,9 @@ QSLC_HD MulConst make_const(double c)
     const int lo = 1 - k.e > 1 ? 1 - k.e : 1;
     const int hi = 2044 - k.e < 2046 ? 2044 - k.e : 2046;
     if (lo > hi) k.usable = 0;
+    // the dot product places a zero product at exponent -1023 + e, below
+    // every normal product only while |c| < 2
+    if (k.e > 0) k.usable = 0;
     k.ef_lo = uint32_t(lo);
     k.ef_span = lo > hi ? 0u : uint32_t(hi - lo);
     return k;
@@ -204,11 +207,10 @@ QSLC_HD uint64_t add_rn(uint64_t x, uint64_t y, bool &ok)
 struct DivConst {
     uint64_t m;      // significand with the hidden bit
     uint64_t rinv;   // floor((2^116 - 1) / m): a 64-bit reciprocal
+    uint32_t r0, r1, r2;   // floor((2^148 - 1) / m), below 2^96: a 96-bit reciprocal, low word first
     int e;           // unbiased exponent
     uint64_t sign;
     int usable;
-    uint64_t half;   // m >> 1: the remainder above it rounds up
-    uint64_t tie;    // 1 when m is even (only then can a remainder equal m / 2)
     // biased exponents of a normal dividend whose quotient stays normal
     uint32_t ef_lo, ef_span;
 };
@@ -225,8 +227,19 @@ inline DivConst make_div(double y)
     k.e = ef - 1023;
     const unsigned __int128 num = ((unsigned __int128)1 << 116) - 1;
     k.rinv = (uint64_t)(num / k.m);
-    k.half = k.m >> 1;
-    k.tie = (k.m & 1) ? 0 : 1;
+    // 2^148 - 1 in base 2^32 is 0xFFFFF followed by four all-ones words;
+    // long division by m keeps every partial remainder below 2^85
+    unsigned __int128 rem = 0;
+    uint32_t q[5];
+    for (int i = 0; i < 5; i++) {
+        const unsigned __int128 cur = (rem << 32) | (i == 0 ? 0xFFFFFu : 0xFFFFFFFFu);
+        q[i] = uint32_t(cur / k.m);
+        rem = cur % k.m;
+    }
+    k.r2 = q[2];
+    k.r1 = q[3];
+    k.r0 = q[4];
+    if (q[0] | q[1]) k.usable = 0;   // cannot happen for m >= 2^52
     // quotient exponent ef - 1023 - e - (0 or 1) must stay in [-1021, 1022]
     const int lo = 3 + k.e > 1 ? 3 + k.e : 1;
     const int hi = 2045 + k.e < 2046 ? 2045 + k.e : 2046;
@@ -237,11 +250,15 @@ inline DivConst make_div(double y)
 }
 
 // RN(x / y), x packed, y a normal constant: the hot form of the division.
-// The quotient significand t = floor(mx * 2^k / my) (k = 52 or 53, so
-// that t has 53 bits) comes from the high part of the full product of mx
-// and the 64-bit reciprocal, which is low by at most one; the exact
-// remainder corrects it once and, against my / 2, rounds it.  The rounding
-// increment goes into the packed result, so a carry moves into the
+// With R = floor((2^148 - 1) / my), H = floor(mx * R / 2^32) is 2^116 * mx / my
+// less under 2^22 + 1: the quotient significand t (53 bits, after one more
+// left shift when mx < my) is its high part, and the next 64 bits v are the
+// fraction that decides the rounding: up when v >= 2^63.  Only a fraction
+// within 2^24 units of v of one half cannot be decided from the estimate
+// (an exact tie always lands there); it declines (ok = false) and the
+// caller divides on the FP64 pipe.  A fraction just below 1 whose true value
+// crossed into the next integer rounds up to that integer either way.  The
+// rounding increment goes into the packed result, so a carry moves into the
 // exponent by itself.
 QSLC_HD uint64_t div_fast(uint64_t x, const DivConst &y, bool &ok)
 {
@@ -251,23 +268,23 @@ QSLC_HD uint64_t div_fast(uint64_t x, const DivConst &y, bool &ok)
     if (((xhi << 1) | xlo) == 0) return uint64_t(sg) << 32;     // +-0 / y
     ok = ok & ((ef - y.ef_lo) <= y.ef_span);
     const uint32_t m1 = (xhi & 0xFFFFFu) | 0x100000u, m0 = xlo;
-    const uint64_t mx = (uint64_t(m1) << 32) | m0;
-    const uint32_t r0 = uint32_t(y.rinv), r1 = uint32_t(y.rinv >> 32);
-    const uint64_t a = uint64_t(m0) * r1, b = uint64_t(m1) * r0;
-    const uint64_t h = (uint64_t(m0) * r0) >> 32;
-    const uint64_t s1 = a + b;
-    const uint64_t s2 = s1 + h;
-    const uint64_t carry = uint64_t(s1 < a) + uint64_t(s2 < s1);
-    const uint64_t hi = uint64_t(m1) * r1 + (s2 >> 32) + (carry << 32);   // product >> 64
-    const uint64_t k53 = uint64_t(mx < y.m);
-    uint64_t t = (hi << k53) | ((s2 >> 31) & k53);            // bit 63 of the product is bit 31 of s2
-    uint64_t r = (mx << (52 + k53)) - t * y.m;
-    const bool c = r >= y.m;
-    t += c ? 1 : 0;
-    r -= c ? y.m : 0;
-    const uint64_t inc = uint64_t(r > y.half) | (uint64_t(r == y.half) & y.tie & (t & 1));
+    // H = a2:a1 words, high part hh: every partial sum below stays under 2^64
+    const uint64_t s1 = uint64_t(m0) * y.r1 + ((uint64_t(m0) * y.r0) >> 32);
+    const uint64_t t1 = uint64_t(m1) * y.r0;
+    const uint64_t a1 = s1 + t1;
+    const uint64_t k1 = uint64_t(a1 < t1);
+    const uint64_t u = uint64_t(m0) * y.r2 + ((k1 << 32) | (a1 >> 32));
+    const uint64_t t2 = uint64_t(m1) * y.r1;
+    const uint64_t a2 = u + t2;
+    const uint64_t k2 = uint64_t(a2 < t2);
+    const uint64_t hh = uint64_t(m1) * y.r2 + ((k2 << 32) | (a2 >> 32));
+    const uint64_t hl = (a2 << 32) | (a1 & 0xFFFFFFFFu);
+    const uint64_t k53 = uint64_t(hh < HIDDEN);
+    const uint64_t t = (hh << k53) | ((hl >> 63) & k53);
+    const uint64_t v = hl << k53;
+    ok = ok & (((v ^ SIGN) + (uint64_t(1) << 24)) >= (uint64_t(1) << 25));
     const int E = int(ef) - 1023 - y.e - int(k53);
-    return (uint64_t(sg) << 32) | ((uint64_t(uint32_t(E + 1022)) << 52) + t + inc);
+    return (uint64_t(sg) << 32) | ((uint64_t(uint32_t(E + 1022)) << 52) + t + (v >> 63));
 }
 
 // RN(x / y) for a normal constant y.  The quotient significand
@@ -478,11 +495,12 @@ QSLC_HD uint64_t div_unp(const Unp &x, const DivConst &y, bool &ok)
 //
 // The code below is the hot form, written for 32-bit integer pipes:
 //  - a product is RN(a * c) with its significand left unnormalised when the
-//    rounding carries out (m = 2^53 then stands for 2^52 at exponent + 1),
-//    and a zero product is m = 0 with an exponent far below any other;
-//  - the sum orders its operands by exponent only.  With equal exponents a
-//    subtraction may come out negative; it is then negated, which is exact
-//    because no bits were shifted out;
+//    rounding carries out (m = 2^53 then stands for 2^52 at exponent + 1).
+//    A zero has no hidden bit, so its product is m = 0 by itself, with the
+//    exponent -1023 + e(c), below that of every normal product because
+//    |c| < 2 (make_const declines larger constants);
+//  - the sum orders its operands by exponent, then significand, so the
+//    larger one comes first and a subtraction never comes out negative;
 //  - it normalises by a single left shift by the count of leading zeros,
 //    which also covers the carry of an addition;
 //  - the rounding increment is added to the packed result, so a carry out
@@ -490,7 +508,8 @@ QSLC_HD uint64_t div_unp(const Unp &x, const DivConst &y, bool &ok)
 // Operands outside the normal range (or whose products or sum would leave
 // it) set ok = false.
 
-// RN(a * c): significand (53 bits, or 2^53), exponent, sign in bit 31.
+// RN(a * c): significand (53 bits, or 2^53; 0 for a zero), exponent, sign
+// in bit 31.
 QSLC_HD void prod_fast(uint64_t a, const MulConst &c, uint64_t &m, int &e, uint32_t &sg, bool &ok)
 {
     const uint32_t ahi = uint32_t(a >> 32), alo = uint32_t(a);
@@ -498,7 +517,7 @@ QSLC_HD void prod_fast(uint64_t a, const MulConst &c, uint64_t &m, int &e, uint3
     sg = (ahi ^ uint32_t(c.sign >> 32)) & 0x80000000u;
     const bool zero = ((ahi << 1) | alo) == 0;
     ok = ok & (zero | ((ef - c.ef_lo) <= c.ef_span));
-    const uint32_t a1 = (ahi & 0xFFFFFu) | 0x100000u;
+    const uint32_t a1 = (ahi & 0xFFFFFu) | (ef ? 0x100000u : 0u);
     const uint64_t p00 = uint64_t(alo) * c.m0, p01 = uint64_t(alo) * c.m1;
     const uint64_t p10 = uint64_t(a1) * c.m0, p11 = uint64_t(a1) * c.m1;
     const uint64_t mid = p01 + p10;
@@ -511,8 +530,8 @@ QSLC_HD void prod_fast(uint64_t a, const MulConst &c, uint64_t &m, int &e, uint3
     q >>= top;
     uint64_t mm = q >> 1;
     mm += (q & 1) & (st | (mm & 1));
-    m = zero ? 0 : mm;
-    e = zero ? -4000 : int(ef) - 1023 + c.e + int(top);
+    m = mm;
+    e = int(ef) - 1023 + c.e + int(top);
 }
 
 QSLC_HD uint64_t dot2_rn(uint64_t a, const MulConst &c, uint64_t b, const MulConst &s, bool neg,
@@ -524,35 +543,31 @@ QSLC_HD uint64_t dot2_rn(uint64_t a, const MulConst &c, uint64_t b, const MulCon
     prod_fast(a, c, mp, ep, sp, ok);
     prod_fast(b, s, mq, eq, sq, ok);
     if (neg) sq ^= 0x80000000u;
-    // x: the operand with the larger exponent
-    const bool sw = eq > ep;
+    // x: the larger operand
+    const bool sw = (eq > ep) | ((eq == ep) & (mq > mp));
     const uint64_t mx = sw ? mq : mp, my = sw ? mp : mq;
     const int ex = sw ? eq : ep, ey = sw ? ep : eq;
-    const uint32_t sx = sw ? sq : sp, sy = sw ? sp : sq;
+    const uint32_t sx = sw ? sq : sp;
     // lead bit at 60 (61 for 2^53), so even the sum of two products that both
-    // rounded up to 2^53 stays below 2^63 and reads as positive; with at
-    // least 8 trailing zeros in both, no bit is dropped unless d > 8, and
-    // then the result keeps its lead within one place of bit 60
+    // rounded up to 2^53 stays below 2^63; with at least 8 trailing zeros in
+    // both, no bit is dropped unless d > 8, and then the result keeps its
+    // lead within one place of bit 60
     const uint64_t X = mx << 8, Yf = my << 8;
     const unsigned dd = unsigned(ex - ey);
     const unsigned d = dd > 63 ? 63 : dd;
     const uint64_t Y = (Yf >> d) | uint64_t((Yf & ((uint64_t(1) << d) - 1)) != 0);
-    const bool sub = (sx ^ sy) != 0;
-    int64_t S = int64_t(sub ? X - Y : X + Y);
-    uint32_t rs = sx;
-    if (S < 0) {                                    // equal exponents, |y| > |x|
-        S = -S;
-        rs ^= 0x80000000u;
-    }
-    if (S == 0) return uint64_t(sub ? 0u : (sx & sy)) << 32;
-    const int lz = clz64(uint64_t(S));              // >= 2
-    const uint64_t N = uint64_t(S) << lz;           // lead bit at 63
+    const bool sub = ((sp ^ sq) & 0x80000000u) != 0;
+    const uint64_t S = sub ? X - Y : X + Y;
+    if (S == 0) return uint64_t(sub ? 0u : (sp & sq)) << 32;
+    const int lz = clz64(S);                        // >= 2
+    const uint64_t N = S << lz;                     // lead bit at 63
     const int E = ex + 3 - lz;
     const uint64_t mr = N >> 11;
-    const uint64_t rb = N & 0x7FF;
-    const uint64_t inc = uint64_t(rb > 0x400) | (uint64_t(rb == 0x400) & (mr & 1));
+    // round to nearest even on the 11 bits below: carry out of rb + 0x3FF + lsb
+    const uint32_t rb = uint32_t(N) & 0x7FFu;
+    const uint32_t inc = (rb + 0x3FFu + (uint32_t(mr) & 1u)) >> 11;
     ok = ok & (E >= -1021) & (E <= 1022);
-    return (uint64_t(rs) << 32) | ((uint64_t(uint32_t(E + 1022)) << 52) + mr + inc);
+    return (uint64_t(sx) << 32) | ((uint64_t(uint32_t(E + 1022)) << 52) + mr + inc);
 }
 
 }  // namespace emu

@@ -84,7 +84,7 @@ __device__ __forceinline__ T dot2(bool em, T a, T k1, const emu::MulConst &e1, T
         if (em) {
             bool ok = (e1.usable & e2.usable) != 0;
             const uint64_t r = emu::dot2_rn(emu::dbits(a), e1, emu::dbits(b), e2, NEG, ok);
-if (ok) return emu::dfrom(r);
+            if (ok) return emu::dfrom(r);
             return dot2_fallback<NEG>(a, k1, b, k2);
         }
     }
@@ -192,8 +192,8 @@ constexpr unsigned PAT_RUNTIME = 0xFFFFFFFFu;
 #define QSLC_ROT_PATTERNS 0u, 0x115u, 0x155u, 0x111u, 0x555u, 0x151u
 #define QSLC_H_PATTERNS 0u, 0x001u, 0x011u
 #define QSLC_DIAG_PATTERNS 0u, 0x011u, 0x001u, 0x111u
-#define QSLC_NP_PAIR_PATTERNS 0u, 0x115u, 0x111u, 0x011u, 0x001u
-#define QSLC_NP_DIAG_PATTERNS 0u, 0x001u, 0x011u
+#define QSLC_NP_PAIR_PATTERNS 0u, 0x115u, 0x155u, 0x111u, 0x011u, 0x001u
+#define QSLC_NP_DIAG_PATTERNS 0u, 0x001u, 0x011u, 0x111u
 
 // Launch `f(std::integral_constant<unsigned, P>{})` with P = pat when pat is
 // one of CANDIDATES, else with PAT_RUNTIME.

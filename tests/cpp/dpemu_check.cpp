@@ -156,7 +156,7 @@ int main(int argc, char **argv)
         // the operand mixes a gate sees: amplitude-like values, zeros,
         // near-cancellation (b*s close to a*c), wide exponent gaps
         for (int rep = 0; rep < 2; rep++) {
-            double a2 = make(-80, 2), c2 = make(-6, 1), b2 = make(-80, 2), s2 = make(-6, 1);
+            double a2 = make(-80, 2), c2 = make(-6, 0), b2 = make(-80, 2), s2 = make(-6, 0);   // |c| < 2, like gate constants
             const int kind = int(rng() % 8);
             if (kind == 0) a2 = (rng() & 1) ? 0.0 : -0.0;
             if (kind == 1) b2 = (rng() & 1) ? 0.0 : -0.0;
@@ -194,12 +194,33 @@ int main(int argc, char **argv)
             if (fails++ < 10) std::printf("div tie %a / %a: got %a want %a\n", xv, yv, dfrom(q), (double)qref);
         }
     }
+    // the division by RN(sqrt(2)) on full random significands: the estimate
+    // decides the rounding itself for all but about 2^-39 of them
+    long declined_sqrt2 = 0;
+    {
+        const DivConst k2 = make_div(1.4142135623730951);
+        for (long i = 0; i < N / 4; i++) {
+            const double xv = dfrom((uint64_t(1023 - 40 + rng() % 44) << 52) | (rng() & MANT) |
+                                    (rng() & 1 ? SIGN : 0));
+            bool okq = true;
+            const uint64_t q = div_fast(dbits(xv), k2, okq);
+            volatile double qref = xv / 1.4142135623730951;
+            if (!okq) declined_sqrt2++;
+            else if (q != dbits(qref)) {
+                if (fails++ < 10) std::printf("div_fast sqrt2 %a: got %a want %a\n", xv, dfrom(q), (double)qref);
+            }
+        }
+    }
+    if (declined_sqrt2 > 0) {
+        std::printf("%ld declined divisions by sqrt(2)\n", declined_sqrt2);
+        return 4;
+    }
     // products that round up to a power of two (significand 2^53 before
     // normalisation), summed with a second product of the same exponent: two
     // such products of one sign make the largest sum the dot product forms
     long carry_cases = 0;
     for (long i = 0; i < N / 20; i++) {
-        const double c3 = make(-6, 1), s3 = make(-6, 1);
+        const double c3 = make(-6, 0), s3 = make(-6, 0);
         const int top_a = int(rng() & 1), top_b = int(rng() & 1);
         uint64_t ma, mb;
         if (!carry_significand(make_const(c3).m, top_a, ma)) continue;
