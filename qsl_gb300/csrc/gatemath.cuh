@@ -192,8 +192,8 @@ constexpr unsigned PAT_RUNTIME = 0xFFFFFFFFu;
 #define QSLC_ROT_PATTERNS 0u, 0x115u, 0x155u, 0x111u, 0x555u, 0x151u
 #define QSLC_H_PATTERNS 0u, 0x001u, 0x011u
 #define QSLC_DIAG_PATTERNS 0u, 0x011u, 0x001u, 0x111u
-#define QSLC_NP_PAIR_PATTERNS 0u, 0x115u, 0x155u, 0x111u, 0x011u, 0x001u
-#define QSLC_NP_DIAG_PATTERNS 0u, 0x001u, 0x011u, 0x111u
+#define QSLC_NP_PAIR_PATTERNS 0u, 0x115u, 0x111u, 0x011u, 0x001u
+#define QSLC_NP_DIAG_PATTERNS 0u, 0x001u, 0x011u
 
 // Launch `f(std::integral_constant<unsigned, P>{})` with P = pat when pat is
 // one of CANDIDATES, else with PAT_RUNTIME.
