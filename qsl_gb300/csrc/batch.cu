@@ -44,9 +44,17 @@ namespace {
 constexpr int MAX_Q = 26;
 // Share of the rotation outputs on the integer pipes (complex128), cycled
 // over a thread's successive pairs: two of four, two of four, one of four;
-// and for rotateZ over the qubits: one of two, one of two, none.
-constexpr unsigned BATCH_PAT_RY = 0x155u;
-constexpr unsigned BATCH_PAT_RZ = 0x011u;
+// and for rotateZ over the qubits: one of two, one of two, none.  The
+// build can set others (-DQSLC_BATCH_PAT_RY=..., -DQSLC_BATCH_PAT_RZ=...)
+// for tuning; the tests hold every setting to the oracle's bits.
+#ifndef QSLC_BATCH_PAT_RY
+#define QSLC_BATCH_PAT_RY 0x155u
+#endif
+#ifndef QSLC_BATCH_PAT_RZ
+#define QSLC_BATCH_PAT_RZ 0x011u
+#endif
+constexpr unsigned BATCH_PAT_RY = QSLC_BATCH_PAT_RY;
+constexpr unsigned BATCH_PAT_RZ = QSLC_BATCH_PAT_RZ;
 
 struct InstDesc {
     uint32_t n, L;
