@@ -44,14 +44,15 @@ namespace {
 constexpr int MAX_Q = 26;
 // Share of the rotation outputs on the integer pipes (complex128), cycled
 // over a thread's successive pairs: two of four, two of four, one of four;
-// and for rotateZ over the qubits: one of two, one of two, none.  The
-// build can set others (-DQSLC_BATCH_PAT_RY=..., -DQSLC_BATCH_PAT_RZ=...)
-// for tuning; the tests hold every setting to the oracle's bits.
+// and for rotateZ one of two on every qubit (measured on GB300 for 4096
+// instances: 3.29 s of kernel time against 3.49 s with one of two on two
+// qubits of three).  The build can set others (-DQSLC_BATCH_PAT_RY=...,
+// -DQSLC_BATCH_PAT_RZ=...) for tuning.
 #ifndef QSLC_BATCH_PAT_RY
 #define QSLC_BATCH_PAT_RY 0x155u
 #endif
 #ifndef QSLC_BATCH_PAT_RZ
-#define QSLC_BATCH_PAT_RZ 0x011u
+#define QSLC_BATCH_PAT_RZ 0x111u
 #endif
 constexpr unsigned BATCH_PAT_RY = QSLC_BATCH_PAT_RY;
 constexpr unsigned BATCH_PAT_RZ = QSLC_BATCH_PAT_RZ;
