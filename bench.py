@@ -472,8 +472,8 @@ def run_gpu(args):
                          if top_name.startswith("k_pair1") else None),
                      "traffic_source": "ncu dram__bytes_read+write of k_pair1 at 26 qubits, "
                                        "scaled by amplitudes (profiles/k_pair1_dense_gates_26q.md)",
-                     "limiter": "FP64 and integer ALU pipes together (80% and 73% active in "
-                                "ncu on a dense state): the reference's rounding costs 12 FP64 "
+                     "limiter": "FP64 pipe (81% active in ncu on a dense state), integer ALU "
+                                "pipe close behind (68%): the reference's rounding costs 12 FP64 "
                                 "operations per amplitude pair; 5 of every 12 outputs run on the "
                                 "integer pipes instead (exact binary64 emulation)"},
         "gpu_launches": launches,
