@@ -42,6 +42,67 @@ static bool carry_significand(uint64_t mc, int top, uint64_t &ma)
     return true;
 }
 
+// x^-1 mod m for x coprime to m (extended Euclid; m < 2^53).
+static uint64_t inverse_mod(uint64_t x, uint64_t m)
+{
+    int64_t r0 = int64_t(m), r1 = int64_t(x % m), t0 = 0, t1 = 1;
+    while (r1 != 0) {
+        const int64_t q = r0 / r1, r2 = r0 - q * r1, t2 = t0 - q * t1;
+        r0 = r1; r1 = r2; t0 = t1; t1 = t2;
+    }
+    return uint64_t(t0 < 0 ? t0 + int64_t(m) : t0);
+}
+
+// Dividends whose quotient by y sits next to a rounding decision: with
+// my odd and k = 52 (mx >= my) or 53 (mx < my), the significand mx with
+// mx * 2^k = r (mod my) leaves the fraction r / my: (my -+ 1) / 2 put it
+// 1 / (2 my) from one half, 0 makes the quotient exact, my - 1 puts it just
+// below the next integer.  The division must decline the first two (no
+// estimate decides them) and get every decided one right.
+static long near_midpoint_cases(double yv, long &declined, long &fails)
+{
+    const DivConst kd = make_div(yv);
+    const uint64_t my = kd.m;
+    long n = 0;
+    for (int k53 = 0; k53 < 2; k53++) {
+        const uint64_t inv = inverse_mod((uint64_t(1) << (52 + k53)) % my, my);
+        const uint64_t rs[5] = {(my - 1) / 2, (my + 1) / 2, 0, my - 1, 1};
+        for (int ri = 0; ri < 5; ri++) {
+            const uint64_t mx0 = uint64_t((unsigned __int128)rs[ri] * inv % my);
+            for (uint64_t j = 0; j < 4; j++) {
+                const uint64_t mx = mx0 + j * my;
+                if (mx < HIDDEN || mx >= 2 * HIDDEN || (mx < my) != (k53 == 1)) continue;
+                for (int e = -30; e <= 2; e += 4) {
+                    for (int sgn = 0; sgn < 2; sgn++) {
+                        const double xv = std::ldexp(double(mx), e - 52) * (sgn ? -1.0 : 1.0);
+                        volatile double qref = xv / yv;
+                        bool ok = true;
+                        const uint64_t q = div_fast(dbits(xv), kd, ok);
+                        n++;
+                        if (!ok) declined++;
+                        if (ok && q != dbits(qref)) {
+                            if (fails++ < 10)
+                                std::printf("div_fast near midpoint %a / %a: got %a want %a\n", xv, yv,
+                                            dfrom(q), (double)qref);
+                        }
+                        if (ri < 2 && ok) {
+                            if (fails++ < 10) std::printf("div_fast decided a midpoint case %a / %a\n", xv, yv);
+                        }
+                        bool ok2 = true;
+                        const uint64_t q2 = div_unp(unpack(dbits(xv), ok2), kd, ok2);
+                        if (ok2 && q2 != dbits(qref)) {
+                            if (fails++ < 10)
+                                std::printf("div_unp near midpoint %a / %a: got %a want %a\n", xv, yv,
+                                            dfrom(q2), (double)qref);
+                        }
+                    }
+                }
+            }
+        }
+    }
+    return n;
+}
+
 int main(int argc, char **argv)
 {
     const long N = argc > 1 ? std::atol(argv[1]) : 20000000;
@@ -209,6 +270,15 @@ int main(int argc, char **argv)
             else if (q != dbits(qref)) {
                 if (fails++ < 10) std::printf("div_fast sqrt2 %a: got %a want %a\n", xv, dfrom(q), (double)qref);
             }
+        }
+    }
+    {
+        long declined_mid = 0;
+        const long n_mid = near_midpoint_cases(1.4142135623730951, declined_mid, fails) +
+                           near_midpoint_cases(1.0 + std::ldexp(1.0, -52) * 12345.0, declined_mid, fails);
+        if (n_mid < 100 || declined_mid == 0) {
+            std::printf("near-midpoint divisions: %ld cases, %ld declined\n", n_mid, declined_mid);
+            return 5;
         }
     }
     if (declined_sqrt2 > 0) {
