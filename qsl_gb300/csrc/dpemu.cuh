@@ -18,12 +18,18 @@
 // Floating-Point Arithmetic, ch. 7-8):
 //   mul: exact 106-bit product of the two 53-bit significands, then
 //        round-to-nearest-even on the guard bit and a sticky bit.
-//   add: align the smaller operand with 10 guard bits, fold every shifted-out
+//   add: align the smaller operand with guard bits, fold every shifted-out
 //        bit into the least significant bit ("jamming"), add or subtract,
-//        renormalise, round to nearest even on the 10 guard bits.  The
-//        jammed bit makes the computed sum odd whenever bits were dropped, so
-//        it can never sit on a rounding tie and always rounds the way the
-//        exact sum does.
+//        renormalise, round to nearest even on the guard bits.  The jammed
+//        bit makes the computed sum odd whenever bits were dropped, so it
+//        can never sit on a rounding tie and always rounds the way the exact
+//        sum does.
+//   div: quotient significand from a precomputed reciprocal of the constant
+//        divisor, the rounding decided from the estimate's fraction bits,
+//        and the few quotients too close to a midpoint declined.
+// Kernels use the hot forms: dot2_rn (a rotation or phase output), div_fast
+// (a Hadamard output), and add_core + div_unp (a Hadamard output with its
+// sum on the integer pipes too).
 #pragma once
 
 #include <cstdint>
@@ -113,6 +119,11 @@ QSLC_HD MulConst make_const(double c)
     k.ef_span = lo > hi ? 0u : uint32_t(hi - lo);
     return k;
 }
+
+// mul_rn, add_rn and div_rn are the plain statements of the three
+// operations, on 64-bit integers and with branches.  No kernel calls them;
+// the CPU check holds them, and the hot forms further down, to the host's
+// IEEE arithmetic.
 
 // RN(a * c) for a normal constant c.  Zeros are exact; the rest needs a
 // normal a and a normal result.
@@ -327,11 +338,10 @@ QSLC_HD uint64_t div_rn(uint64_t x, const DivConst &y, bool &ok)
 }
 
 // ---------------------------------------------------------------------------
-// The dot-product path.  A rounded product stays unpacked -- sign, exponent,
-// 53-bit significand -- and goes straight into the sum, so no product is
-// packed into IEEE bits and unpacked again.  The product is built from four
-// 32 x 32 -> 64 partial products, and every shift is by a constant; the sum
-// normalises add and subtract the same way, without branches on the signs.
+// The unpacked path of a Hadamard output whose sum also runs on the integer
+// pipes: RN(RN(a +- b) / y) as div_unp(add_core(unpack(a), unpack(+-b))),
+// with the sum handed to the division unpacked -- sign, exponent, 53-bit
+// significand -- instead of packed into IEEE bits and unpacked again.
 // ---------------------------------------------------------------------------
 
 // value = m * 2^(e - 52) with m in [2^52, 2^53), or zero when m == 0
@@ -340,43 +350,6 @@ struct Unp {
     int e;
     uint64_t sign;   // SIGN or 0
 };
-
-// RN(a * c), unpacked.  Declines (ok = false) a subnormal, infinite or NaN
-// operand and a product outside the normal range.
-QSLC_HD Unp mul_unp(uint64_t a, const MulConst &c, bool &ok)
-{
-    Unp r;
-    r.sign = (a ^ c.sign) & SIGN;
-    const uint32_t ahi = uint32_t(a >> 32), alo = uint32_t(a);
-    if (((ahi & 0x7FFFFFFFu) | alo) == 0) {        // +-0 * c
-        r.m = 0;
-        r.e = 0;
-        return r;
-    }
-    const int ef = int((ahi >> 20) & 0x7FF);
-    ok = ok & (ef != 0) & (ef != 0x7FF);
-    const uint32_t a1 = (ahi & 0xFFFFFu) | 0x100000u;
-    const uint64_t p00 = uint64_t(alo) * c.m0, p01 = uint64_t(alo) * c.m1;
-    const uint64_t p10 = uint64_t(a1) * c.m0, p11 = uint64_t(a1) * c.m1;
-    const uint64_t mid = p01 + p10;                 // < 2^54
-    const uint64_t lo = p00 + (mid << 32);
-    const uint64_t hi = p11 + (mid >> 32) + uint64_t(lo < p00);   // product = hi:lo < 2^106
-    const uint64_t top = hi >> 41;                  // leading bit at 105 (else at 104)
-    uint64_t q = (hi << 13) | (lo >> 51);           // product >> 51
-    uint64_t st = uint64_t((lo & ((uint64_t(1) << 51) - 1)) != 0);
-    st |= q & top;                                  // with the lead at 105, bit 51 is sticky too
-    q >>= top;
-    uint64_t m = q >> 1;
-    m += (q & 1) & (st | (m & 1));                  // round to nearest even
-    int e = ef - 1023 + c.e + int(top);
-    const uint64_t carry = m >> 53;
-    m >>= carry;
-    e += int(carry);
-    ok = ok & (e >= -1022) & (e <= 1023);
-    r.m = m;
-    r.e = e;
-    return r;
-}
 
 // IEEE bits to the unpacked form; declines subnormals, infinities, NaNs.
 QSLC_HD Unp unpack(uint64_t a, bool &ok)
@@ -394,12 +367,6 @@ QSLC_HD Unp unpack(uint64_t a, bool &ok)
     r.m = (a & MANT) | HIDDEN;
     r.e = ef - 1023;
     return r;
-}
-
-QSLC_HD uint64_t pack(const Unp &x)
-{
-    if (x.m == 0) return x.sign;
-    return x.sign | (uint64_t(x.e + 1023) << 52) | (x.m & MANT);
 }
 
 // RN(x + y) of two unpacked values, still unpacked (a zero keeps its sign).
@@ -446,9 +413,6 @@ QSLC_HD Unp add_core(Unp x, Unp y, bool &ok)
     r.sign = x.sign;
     return r;
 }
-
-// RN(x + y) of two unpacked values, packed into IEEE bits.
-QSLC_HD uint64_t add_unp(const Unp &x, const Unp &y, bool &ok) { return pack(add_core(x, y, ok)); }
 
 // RN(x / y) for an unpacked x and a normal constant y, packed.  The
 // quotient significand t = floor(mx * 2^k / my) (k = 52 when mx >= my, else
