@@ -282,6 +282,23 @@ def run_np(args, torch, q, stream):
     return out
 
 
+BATCH_SHOTS = 1024
+
+
+def batch_workload(args):
+    """The batch section's instances: n uniform in [10, 20], L uniform in
+    [4, 16], angles uniform in [0, 2 pi), 1024 uniforms per instance.
+    Returns the generator too, which the plain comparison draws from next."""
+    rng = np.random.default_rng(SEED + 8)
+    ninst = args.batch_instances
+    ns = rng.integers(10, 21, ninst).astype(np.uint32)
+    ls = rng.integers(4, 17, ninst).astype(np.uint32)
+    gates = ls.astype(np.int64) * (3 * ns.astype(np.int64) - 1)
+    angles = rng.uniform(0, 2 * np.pi, int(np.sum(2 * ns.astype(np.int64) * ls)))
+    u = workloads.uniforms(ninst * BATCH_SHOTS, SEED + 9)
+    return rng, ns, ls, gates, angles, u
+
+
 def run_batch(args, torch, q):
     """The batching form: 4096 independent ansatz circuits, n uniform in
     [10, 20], L uniform in [4, 16] layers of rotateY/rotateZ on every qubit
@@ -289,14 +306,9 @@ def run_batch(args, torch, q):
     probabilities and 1024 shots per instance; one persistent launch from a
     CUDA graph, complex64 and complex128.  The plain FP64 path (per-gate
     launches through the C ABI) runs a random subset of the same instances."""
-    rng = np.random.default_rng(SEED + 8)
-    ninst, nshots = args.batch_instances, 1024
-    ns = rng.integers(10, 21, ninst).astype(np.uint32)
-    ls = rng.integers(4, 17, ninst).astype(np.uint32)
-    gates = ls.astype(np.int64) * (3 * ns.astype(np.int64) - 1)
+    rng, ns, ls, gates, angles, u = batch_workload(args)
+    ninst, nshots = args.batch_instances, BATCH_SHOTS
     total_gates = int(gates.sum())
-    angles = rng.uniform(0, 2 * np.pi, int(np.sum(2 * ns.astype(np.int64) * ls)))
-    u = workloads.uniforms(ninst * nshots, SEED + 9)
     out = {"instances": ninst, "shots_per_instance": nshots, "total_gates": total_gates,
            "state_bytes_c128": int(np.sum((1 << ns.astype(np.int64)) * 16))}
     for name, dt in (("c64", np.complex64), ("c128", np.complex128)):
@@ -339,6 +351,47 @@ def run_batch(args, torch, q):
     out["plain_sample_instances"] = int(args.batch_plain_sample)
     out["speedup_c64_vs_plain_fp64"] = out["c64"]["gates_per_s"] / plain_gps
     out["speedup_c128_vs_plain_fp64"] = out["c128"]["gates_per_s"] / plain_gps
+    return out
+
+
+def run_batch_sharded(args, torch, q, rep):
+    """The batch section on several ranks: the same instances, split by
+    cost (qsl_gb300/batch_shards.py), each rank's share as one batch on its
+    GPU.  The job's rate is all instances' gates over the slowest rank's
+    time; every probability and shot is gathered back in instance order
+    after the timed region, and rank 0 checks that every instance came
+    back."""
+    from qsl_gb300 import batch_shards as bs
+    _, ns, ls, gates, angles, u = batch_workload(args)
+    ninst, nshots = args.batch_instances, BATCH_SHOTS
+    total_gates = int(gates.sum())
+    parts = bs.partition_by_cost(bs.instance_costs(ns, ls), rep.world)
+    mine = parts[rep.rank]
+    sub_n, sub_l, sub_a, sub_u = bs.select(ns, ls, angles, u, nshots, mine)
+    loads = [int(bs.instance_costs(ns[p], ls[p]).sum()) for p in parts]
+    out = {"instances": ninst, "shots_per_instance": nshots, "total_gates": total_gates,
+           "ranks": rep.world, "partition": "longest first by L * 2^n",
+           "max_over_mean_load": max(loads) / (sum(loads) / len(loads))}
+    empty = ([], np.empty((0, nshots), dtype=np.uint64))
+    for name, dt in (("c64", np.complex64), ("c128", np.complex128)):
+        b = q.Batch(sub_n, sub_l, nshots, dtype=dt) if mine.size else None
+        tuned_ms = b.autotune(sub_a, sub_u) if b else 0.0
+        if b:
+            b.run(sub_a, sub_u)                           # warm-up replay
+        rep.barrier()
+        torch.cuda.synchronize()
+        reps = 2
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            res = b.run(sub_a, sub_u) if b else empty
+        torch.cuda.synchronize()
+        slowest = rep.max((time.perf_counter() - t0) / reps)
+        got = rep.gather(([np.asarray(x) for x in res[0]], np.asarray(res[1])))
+        probs, _ = bs.assemble(ns, nshots, parts, got)
+        assert all(p.shape == (int(n), 2) for p, n in zip(probs, ns))
+        out[name] = {"s": slowest, "gates_per_s": total_gates / slowest,
+                     "kernel_ms_slowest_rank": rep.max(tuned_ms)}
+        del b
     return out
 
 
@@ -488,7 +541,8 @@ def run_gpu(args):
     if not args.no_np:
         line["np"] = run_np(args, torch, q, stream)
     if not args.no_batch:
-        line["batch"] = run_batch(args, torch, q)
+        line["batch"] = (run_batch(args, torch, q) if world == 1
+                         else run_batch_sharded(args, torch, q, rep))
     if rank == 0 and not args.no_cpu:
         v, done, thr = cpu_sample(circ, n, seconds=args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": thr, "kind": "port",

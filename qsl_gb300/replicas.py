@@ -54,6 +54,15 @@ class Replicas:
     def sum(self, x: float) -> float:
         return self._reduce(x, "SUM")
 
+    def gather(self, obj) -> list:
+        """Every rank's `obj` (any picklable value), in rank order, on every
+        rank: one all-gather, outside any timed region."""
+        if not self.dist:
+            return [obj]
+        out = [None] * self.world
+        self.dist.all_gather_object(out, obj)
+        return out
+
     def throughput(self, units: float, seconds: float) -> float:
         """All ranks' units over the slowest rank's seconds."""
         return self.sum(units) / self.max(seconds)
