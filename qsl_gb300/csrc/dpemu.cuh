@@ -523,7 +523,7 @@ QSLC_HD uint64_t dot2_rn(uint64_t a, const MulConst &c, uint64_t b, const MulCon
     const bool sub = ((sp ^ sq) & 0x80000000u) != 0;
     const uint64_t S = sub ? X - Y : X + Y;
     if (S == 0) return uint64_t(sub ? 0u : (sp & sq)) << 32;
-    const int lz = clz64(S);                        // >= 2
+    const int lz = clz64(S);                        // >= 1: S <= 2^61 + 2^61
     const uint64_t N = S << lz;                     // lead bit at 63
     const int E = ex + 3 - lz;
     const uint64_t mr = N >> 11;
