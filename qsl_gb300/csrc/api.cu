@@ -469,7 +469,8 @@ int qslc_prob(qslc_state *s, unsigned targ, unsigned outcome, double *out)
     int rc = check_handle(s);
     if (!rc) rc = check_q(s, targ);
     if (rc) return rc;
-    if (outcome > 1 || !out) return fail(QSLC_EINVAL, "outcome must be 0 or 1");
+    if (outcome > 1) return fail(QSLC_EINVAL, "outcome must be 0 or 1");
+    if (!out) return fail(QSLC_EINVAL, "null output pointer");
     rc = flushed(s);
     if (rc) return rc;
     return s->np ? np_prob(s, targ, outcome, out) : seq_prob(s, targ, outcome, out);
