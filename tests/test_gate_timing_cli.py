@@ -1,0 +1,27 @@
+"""The dense-state gate timer's command line (qsl_gb300/gate_timing.py):
+argument checks that need no GPU."""
+import pytest
+
+from qsl_gb300 import gate_timing
+
+
+def test_rejects_targets_outside_the_state():
+    with pytest.raises(SystemExit):
+        gate_timing.main(["--qubits", "10", "--targets", "3,10"])
+    with pytest.raises(SystemExit):
+        gate_timing.main(["--qubits", "10", "--targets", "-1"])
+
+
+def test_prepare_dense_touches_every_qubit_twice():
+    calls = []
+
+    class Rec:
+        def rotateY(self, q, a):
+            calls.append(("rotateY", q, a))
+
+        def rotateZ(self, q, a):
+            calls.append(("rotateZ", q, a))
+
+    gate_timing.prepare_dense(Rec(), 5)
+    assert [c[:2] for c in calls] == [(g, q) for q in range(5) for g in ("rotateY", "rotateZ")]
+    assert all(0.3 <= c[2] <= 2.8 for c in calls)
