@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(TC_M) k_dense_tc(float2 *__restrict__ st, uint
 #pragma unroll
             for (int v = 0; v < 32; v++) a[v] = st[bn | s_off[v]];
         }
-        // one thread polls the barrier (bounded); the block follows its verdict
+        // one thread polls the barrier (bounded); the block follows its outcome
         if (tid == 0) arrived = mbar_wait(mbar_s, phase) ? 1 : 0;
         __syncthreads();
         if (!arrived) {
