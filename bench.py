@@ -24,7 +24,10 @@ cpu_baseline the oracle (a C restatement of the reference's OpenMP backend)
 
 `--impl reference` times that CPU implementation alone (the reference
 cannot be built on the GPU machine), with every host thread, on the same
-config and metric; its step is a bounded sample of a layer (see --ref-gates).
+config and metric: the same W untimed and K timed layers.
+
+`--gpus N` with no launcher around it starts N ranks itself (one per GPU,
+under torch.distributed.run); each rank runs an independent replica.
 """
 from __future__ import annotations
 
@@ -74,11 +77,11 @@ def kernel_of(gate: str) -> str:
             "controlPhase": "k_diag2<PHASE>"}[gate]
 
 
-# DRAM bytes per launch over algorithmic bytes for the dense one-qubit
-# kernels, from the ncu capture summarised in
-# profiles/k_pair1_dense_gates_26q.md (2.086 GB moved for 2.147 GB of
-# algorithmic traffic at 26 qubits on a dense state; it scales with the
-# amplitude count).
+# DRAM bytes per launch over algorithmic bytes of the dense one-qubit
+# kernel, from an ncu capture of k_pair1 on a dense 26-qubit state (2.086 GB
+# moved for 2.147 GB of algorithmic traffic; the traffic scales with the
+# amplitude count).  It is not measured by this program: the JSON line says
+# so next to the number, and --traffic replaces it with a capture's figure.
 K_PAIR1_TRAFFIC_RATIO = 2.086 / 2.147
 
 
@@ -359,8 +362,8 @@ def run_batch_sharded(args, torch, q, rep):
     cost (qsl_gb300/batch_shards.py), each rank's share as one batch on its
     GPU.  The job's rate is all instances' gates over the slowest rank's
     time; every probability and shot is gathered back in instance order
-    after the timed region, and rank 0 checks that every instance came
-    back."""
+    after the timed region, and rank 0 then runs the whole batch alone and
+    reports whether the reassembled results are its bits."""
     from qsl_gb300 import batch_shards as bs
     _, ns, ls, gates, angles, u = batch_workload(args)
     ninst, nshots = args.batch_instances, BATCH_SHOTS
@@ -387,11 +390,64 @@ def run_batch_sharded(args, torch, q, rep):
         torch.cuda.synchronize()
         slowest = rep.max((time.perf_counter() - t0) / reps)
         got = rep.gather(([np.asarray(x) for x in res[0]], np.asarray(res[1])))
-        probs, _ = bs.assemble(ns, nshots, parts, got)
-        assert all(p.shape == (int(n), 2) for p, n in zip(probs, ns))
+        probs, shots = bs.assemble(ns, nshots, parts, got)
         out[name] = {"s": slowest, "gates_per_s": total_gates / slowest,
                      "kernel_ms_slowest_rank": rep.max(tuned_ms)}
         del b
+        if rep.leader:
+            # the whole batch on this rank alone, after the timed region: the
+            # reassembled results must be its bits, instance for instance
+            whole = q.Batch(ns, ls, nshots, dtype=dt)
+            p1, s1 = whole.run(angles, u)
+            same = (all(np.array_equal(a, c) for a, c in zip(probs, p1))
+                    and np.array_equal(np.asarray(shots), np.asarray(s1)))
+            out[name]["matches_single_rank_run"] = bool(same)
+            del whole
+        rep.barrier()
+    return out
+
+
+def workload_config(n, steps, warmup, layers):
+    """The `config` object, the same in both arms: the circuit, its size and
+    the gates the K timed steps run."""
+    ngates = sum(len(layers[(warmup + k) % len(layers)]) for k in range(steps))
+    return {"workload": f"plain FP64 {n}-qubit layered random circuit (depth {LAYERS}): per layer "
+                        f"{n} one-qubit gates + {n // 2} controlNot/controlPhase; one layer per step, "
+                        f"layers {warmup}..{warmup + steps - 1} timed after {warmup} untimed",
+            "nqubits": n, "state_bytes": (1 << n) * 16, "gates_timed": ngates,
+            "l2": f"state ({(1 << n) * 16 / 2**30:g} GiB) is larger than L2 (129 MB); no flush needed"}
+
+
+def e2e_pinned(n, local_ranks):
+    """Whether every local rank may pin a host copy of its state."""
+    try:
+        ram = os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_PHYS_PAGES")
+    except (ValueError, OSError):
+        return local_ranks == 1
+    return local_ranks * (1 << n) * 16 <= ram // 2
+
+
+def roofline_of(args, name, top, peak, peak_kind):
+    """The roofline object of the dominant kernel: its algorithmic bytes per
+    launch over its mean CUDA-event launch time, against the measured HBM
+    copy bandwidth.  `traffic` is DRAM bytes per launch: --traffic when a
+    capture of this run's kernel is given, else the dense-state ratio of an
+    earlier capture scaled to this launch, and labelled as such."""
+    per_launch = top["bytes"] / top["launches"]
+    achieved = per_launch / (top["ms"] / top["launches"] * 1e-3) / 1e9
+    out = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+           "frac": achieved / peak, "peak_source": peak_kind,
+           "alg_bytes_per_launch": per_launch}
+    if args.traffic:
+        out["traffic"] = args.traffic
+        out["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, given with --traffic"
+    elif name.startswith("k_pair1"):
+        out["traffic"] = per_launch * K_PAIR1_TRAFFIC_RATIO
+        out["traffic_source"] = ("scaled from an earlier ncu capture of k_pair1 on a dense 26-qubit "
+                                 "state (DRAM bytes / algorithmic bytes = 0.972); not measured in this run")
+    else:
+        out["traffic"] = None
+        out["traffic_source"] = "no capture of this kernel given"
     return out
 
 
@@ -459,7 +515,6 @@ def run_gpu(args):
     gate_ms = sum(d["ms"] for d in per.values())
     top_name, top = max(per.items(), key=lambda kv: kv[1]["ms"])
     peak, peak_kind = peaks()
-    achieved = top["bytes"] / top["launches"] / (top["ms"] / top["launches"] * 1e-3) / 1e9
     all_gbs = sum(d["bytes"] for d in per.values()) / (gate_ms * 1e-3) / 1e9
 
     # measurement and sampling on the evolved state
@@ -477,7 +532,10 @@ def run_gpu(args):
     # end to end through the C ABI with host buffers
     e2e = None
     if not args.no_e2e:
-        host = torch.empty((1 << n) * 2, dtype=torch.float64, pin_memory=True)
+        # pinned host memory for every local rank's 16 GiB state only while
+        # that stays under half of the host's memory; pageable above that
+        pinned = e2e_pinned(n, int(os.environ.get("LOCAL_WORLD_SIZE", world)))
+        host = torch.empty((1 << n) * 2, dtype=torch.float64, pin_memory=pinned)
         hv = host.numpy().view(np.complex128)
         hv[:] = 0
         hv[0] = 1
@@ -496,7 +554,8 @@ def run_gpu(args):
         e2e = {"value": g2 / (e1 - e0), "unit": UNIT,
                "h2d_bytes_per_step": int(hv.nbytes / args.steps),
                "d2h_bytes_per_step": int((sh2.nbytes + 8 * len(o2)) / args.steps),
-               "includes": "qslc_set_state of the 16 GiB state from pinned host memory, K layers, "
+               "includes": f"qslc_set_state of the {(1 << n) * 16 >> 30} GiB state from "
+                           f"{'pinned' if pinned else 'pageable'} host memory, K layers, "
                            "8 measurements, 100k-shot sampleAll read back"}
         del sim2, host
 
@@ -505,12 +564,9 @@ def run_gpu(args):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {
-            "workload": f"plain FP64 {n}-qubit layered random circuit (depth {LAYERS}): per layer "
-                        f"{n} one-qubit gates + {n // 2} controlNot/controlPhase; one layer per step",
-            "nqubits": n, "state_bytes": (1 << n) * 16, "gates_timed": ngates,
-            "parallelism": "replicas" if world > 1 else "single GPU",
-            "l2": "state (16 GiB) is larger than L2 (129 MB); no flush needed",
+        "config": workload_config(n, args.steps, args.warmup, layers),
+        "parallelism": "replicas" if world > 1 else "single GPU",
+        "detail": {
             "hbm_gbs_all_gates": all_gbs,
             "measure8_ms": (t1 - t0) * 1e3, "measure_outcomes": outs,
             "sample_shots": args.shots, "sample_ms": (t2 - t1) * 1e3,
@@ -518,17 +574,7 @@ def run_gpu(args):
                             "gbs": v["bytes"] / (v["ms"] * 1e-3) / 1e9,
                             "share": v["ms"] / gate_ms} for k, v in per.items()},
         },
-        "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": args.traffic if args.traffic else (
-                         top["bytes"] / top["launches"] * K_PAIR1_TRAFFIC_RATIO
-                         if top_name.startswith("k_pair1") else None),
-                     "traffic_source": "ncu dram__bytes_read+write of k_pair1 at 26 qubits, "
-                                       "scaled by amplitudes (profiles/k_pair1_dense_gates_26q.md)",
-                     "limiter": "FP64 pipe (81% active in ncu on a dense state), integer ALU "
-                                "pipe close behind (68%): the reference's rounding costs 12 FP64 "
-                                "operations per amplitude pair; 5 of every 12 outputs run on the "
-                                "integer pipes instead (exact binary64 emulation)"},
+        "roofline": roofline_of(args, top_name, top, peak, peak_kind),
         "gpu_launches": launches,
         "clocks": clk,
     }
@@ -554,8 +600,13 @@ def run_gpu(args):
 
 
 def run_reference(args):
-    """The reference's CPU algorithm (its C restatement: the reference itself
-    does not build on the GPU machine) on every host thread."""
+    """The reference's CPU algorithm on every host thread: the oracle's C
+    restatement of the reference's OpenMP backend (the reference's own
+    sources are not on the GPU machine).  It runs the GPU arm's workload
+    exactly: the same circuit, W untimed layers, then K timed layers of 45
+    gates each, on a state that starts at |0...0>.  --ref-gates G > 0 bounds
+    a step to the first G gates of its layer instead (the config then says
+    so)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -566,34 +617,53 @@ def run_reference(args):
     layers = layers_of(circ, n)
     threads = os.cpu_count() or 1
     sim = oracle.PortQubits(n, nthreads=threads)
-    sim.gate("rotateX", 0, None, 0.1)
-    per_step = max(1, args.ref_gates)
-    k = 0
+    per_step = args.ref_gates if args.ref_gates > 0 else None
 
     def step(li):
-        for g in layers[li % len(layers)][:per_step]:
+        gates = layers[li % len(layers)][:per_step]
+        for g in gates:
             sim.gate(*g)
+        return len(gates)
 
     for w in range(args.warmup):
         step(w)
+    k = 0
     t0 = time.perf_counter()
     for s in range(args.steps):
-        step(args.warmup + s)
-        k += min(per_step, len(layers[(args.warmup + s) % len(layers)]))
+        k += step(args.warmup + s)
     dt = time.perf_counter() - t0
     v = k / dt
+    config = workload_config(n, args.steps, args.warmup, layers)
+    if per_step:
+        config["workload"] += f"; reference arm: the first {per_step} gates of each layer only"
+        config["gates_timed"] = k
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic",
-        "config": {"workload": f"plain FP64 {n}-qubit layered random circuit (depth {LAYERS}), "
-                               f"the first {per_step} gates of each layer per step",
-                   "nqubits": n},
+        "data": "synthetic", "config": config, "parallelism": f"OpenMP, {threads} host threads",
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{k} gates: the first {per_step} gates of {args.steps} layers"},
+                         "sample": f"{k} gates: {'the first %d gates of ' % per_step if per_step else ''}"
+                                   f"layers {args.warmup}..{args.warmup + args.steps - 1}"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
+
+
+def free_port() -> int:
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        return sk.getsockname()[1]
+
+
+def launch_ranks(nranks: int, argv, script: str | None = None) -> int:
+    """Start `nranks` local ranks of `script` (this file by default) under
+    torch.distributed.run, one per GPU (each rank binds LOCAL_RANK), with the
+    rendezvous on 127.0.0.1; returns the launcher's exit status."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+           f"--nproc-per-node={nranks}", "--master-addr", "127.0.0.1",
+           "--master-port", str(free_port()), script or os.path.abspath(__file__), *argv]
+    return subprocess.call(cmd)
 
 
 def main():
@@ -605,7 +675,8 @@ def main():
     ap.add_argument("--qubits", type=int, default=N_QUBITS)
     ap.add_argument("--shots", type=int, default=100_000)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--ref-gates", type=int, default=2)
+    ap.add_argument("--ref-gates", type=int, default=0,
+                    help="reference arm: time only the first G gates of each layer (0: whole layers)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fused", action="store_true")
@@ -620,6 +691,9 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # --gpus N without a launcher: start N ranks here, one per GPU
+        sys.exit(launch_ranks(args.gpus, sys.argv[1:]))
     if args.impl == "reference":
         run_reference(args)
     else:

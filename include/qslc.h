@@ -287,9 +287,13 @@ QSLC_API int qslc_batch_destroy(qslc_batch *b);
  * that loads the library holds until the process exits, shared by all
  * calls (calls that overlap on the GPU race on it; calls made through this
  * library in one process are serialised).  States above
- * QSLC_NOALLOC_MAX_QUBITS qubits are rejected with QSLC_EINVAL.  The first
- * call on a device looks up the array's address on that device; make it
- * before any stream capture. */
+ * QSLC_NOALLOC_MAX_QUBITS qubits (and nqubits == 0) are rejected with
+ * QSLC_EINVAL before anything else is done.  Each call blocks until the
+ * result is on the host: it synchronises `stream` and copies into fixed
+ * host arrays, so it must not be called while that stream (or, in global
+ * capture mode, any stream) is being captured.  The first call on a device
+ * looks up the array's address on that device and keeps it for the life of
+ * the process; do not use the library across a cudaDeviceReset. */
 #define QSLC_NOALLOC_SCRATCH_BYTES (1u << 20)
 #define QSLC_NOALLOC_MAX_QUBITS 27
 QSLC_API int qslc_prob_noalloc(const void *amps, unsigned nqubits, int dtype, unsigned targ,

@@ -26,7 +26,23 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "libqsl_port.so")
 REF_SO = os.path.join(HERE, "_ref", "libqslref.so")
-REF_SRC = os.environ.get("QSL_REFERENCE_SRC", "/root/reference")
+
+
+def _ref_src() -> str:
+    """The reference's source tree: QSL_REFERENCE_SRC, else the default that
+    oracle/Makefile holds (asked for with `make -s print-ref`)."""
+    env = os.environ.get("QSL_REFERENCE_SRC")
+    if env:
+        return env
+    try:
+        out = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True,
+                             text=True, timeout=60)
+        return out.stdout.strip() if out.returncode == 0 else ""
+    except (OSError, subprocess.SubprocessError):
+        return ""
+
+
+REF_SRC = _ref_src()
 
 ONE_QUBIT = ("pauliX", "pauliY", "pauliZ", "hadamard", "phase", "rotateX", "rotateY", "rotateZ")
 ANGLED = {"phase", "rotateX", "rotateY", "rotateZ", "controlRotateX", "controlRotateY",
@@ -50,7 +66,7 @@ def build(reference: bool | None = None, quiet: bool = True) -> None:
     """Build the restatement, and the reference library when its sources exist."""
     targets = ["port"]
     if reference is None:
-        reference = os.path.isdir(os.path.join(REF_SRC, "src", "qubits"))
+        reference = bool(REF_SRC) and os.path.isdir(os.path.join(REF_SRC, "src", "qubits"))
     if reference:
         targets.append("ref")
     jobs = str(max(1, min(16, os.cpu_count() or 1)))

@@ -22,8 +22,14 @@
 //     its result before returning, but the scratch must not be shared with
 //     anything else;
 //   * the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress) with that device current, once per device;
-//     make that first call before any stream capture begins.
+//     (cudaGetSymbolAddress) with that device current, once per device, and
+//     keeps it for the life of the process: a cudaDeviceReset (or any other
+//     end of the device's primary context) invalidates it, so the library
+//     must not be used across a device reset;
+//   * every call waits for its result on the host (it synchronises its
+//     stream and copies small results into fixed host arrays), so no call
+//     may be made while its stream -- or, in global capture mode, any
+//     stream -- is being captured into a CUDA graph.
 #include <mutex>
 
 #include "seqsum.cuh"
@@ -86,13 +92,15 @@ extern "C" int qslc_prob_noalloc(const void *amps, unsigned nqubits, int dtype, 
     if (!amps || !out) return fail(QSLC_EINVAL, "null pointer");
     if (dtype != QSLC_C128 && dtype != QSLC_C64) return fail(QSLC_EINVAL, "unknown dtype");
     if (outcome > 1) return fail(QSLC_EINVAL, "outcome must be 0 or 1");
-    if (nqubits < 1 || targ >= nqubits)
-        return fail(QSLC_EINVAL, "qubit index out of range");
-    if ((uint64_t(1) << (nqubits - 1)) > NOALLOC_MAX_TERMS)
-        return fail(QSLC_EINVAL, "qslc_prob_noalloc accepts at most " +
+    // the qubit count is bounded before it is used in any shift
+    if (nqubits < 1 || nqubits > QSLC_NOALLOC_MAX_QUBITS)
+        return fail(QSLC_EINVAL, "qslc_prob_noalloc accepts 1 to " +
                                      std::to_string(QSLC_NOALLOC_MAX_QUBITS) +
                                      " qubits (its fixed scratch is " +
                                      std::to_string(QSLC_NOALLOC_SCRATCH_BYTES) + " bytes)");
+    if (targ >= nqubits) return fail(QSLC_EINVAL, "qubit index out of range");
+    static_assert((uint64_t(1) << (QSLC_NOALLOC_MAX_QUBITS - 1)) <= NOALLOC_MAX_TERMS,
+                  "the host arrays hold the largest accepted state");
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
     int dev = 0;
     QSLC_CUDA(cudaGetDevice(&dev));

@@ -142,7 +142,16 @@ class _StubBatch:
         return fake_runner(self.ns, self.ls, angles, uniforms)
 
 
-def _bench_rank_main(rank: int, world: int, port: int, out):
+class _PositionalStubBatch(_StubBatch):
+    """A faulty batch: an instance's shots depend on its position within
+    the batch, so a share run alone differs from the whole batch."""
+
+    def run(self, angles, uniforms):
+        probs, shots = fake_runner(self.ns, self.ls, angles, uniforms)
+        return probs, shots + np.arange(len(self.ns), dtype=np.uint64)[:, None]
+
+
+def _bench_rank_main(rank: int, world: int, port: int, out, stub=_StubBatch):
     import sys
     import types
     os.environ.update(RANK=str(rank), WORLD_SIZE=str(world), LOCAL_RANK=str(rank),
@@ -151,7 +160,7 @@ def _bench_rank_main(rank: int, world: int, port: int, out):
     import bench
     from qsl_gb300.replicas import Replicas
     rep = Replicas("gloo")
-    q = types.SimpleNamespace(Batch=_StubBatch)
+    q = types.SimpleNamespace(Batch=stub)
     torch = types.SimpleNamespace(cuda=types.SimpleNamespace(synchronize=lambda: None))
     args = types.SimpleNamespace(batch_instances=40)
     res = bench.run_batch_sharded(args, torch, q, rep)
@@ -159,22 +168,38 @@ def _bench_rank_main(rank: int, world: int, port: int, out):
     rep.close()
 
 
-def test_bench_batch_section_on_two_ranks():
-    """bench.py's batch section with two ranks: both report the same job
-    (all instances' gates over the slowest rank) and a balanced split."""
-    pytest.importorskip("torch.distributed")
+def _two_bench_ranks(stub):
     ctx = mp.get_context("spawn")
     out = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_bench_rank_main, args=(r, 2, port, out)) for r in range(2)]
+    procs = [ctx.Process(target=_bench_rank_main, args=(r, 2, port, out, stub)) for r in range(2)]
     for p in procs:
         p.start()
     res = sorted(out.get(timeout=180) for _ in procs)
     for p in procs:
         p.join(timeout=60)
         assert p.exitcode == 0
-    (_, a), (_, b) = res
+    return res
+
+
+def test_bench_batch_section_on_two_ranks():
+    """bench.py's batch section with two ranks: both report the same job
+    (all instances' gates over the slowest rank) and a balanced split, and
+    rank 0 finds the reassembled results equal to a single-rank run."""
+    pytest.importorskip("torch.distributed")
+    (_, a), (_, b) = _two_bench_ranks(_StubBatch)
     assert a["ranks"] == b["ranks"] == 2 and a["instances"] == 40
     for k in ("c64", "c128"):
         assert a[k]["s"] == b[k]["s"] and a[k]["gates_per_s"] == a["total_gates"] / a[k]["s"]
+        assert a[k]["matches_single_rank_run"] is True
+        assert "matches_single_rank_run" not in b[k]
     assert a["max_over_mean_load"] < 1.5
+
+
+def test_bench_batch_section_reports_a_mismatch():
+    """A batch whose results depend on the batch around an instance gives
+    different bits when split: rank 0's check reports it."""
+    pytest.importorskip("torch.distributed")
+    (_, a), _ = _two_bench_ranks(_PositionalStubBatch)
+    for k in ("c64", "c128"):
+        assert a[k]["matches_single_rank_run"] is False

@@ -10,11 +10,12 @@ import subprocess
 import numpy as np
 import pytest
 
+import oracle
 from conftest import bits
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CPP = os.path.join(ROOT, "tests", "cpp")
-REF_INC = os.path.join(os.environ.get("QSL_REFERENCE_SRC", "/root/reference"), "include")
+REF_INC = os.path.join(oracle.REF_SRC, "include") if oracle.REF_SRC else ""
 
 
 def gxx(*args):

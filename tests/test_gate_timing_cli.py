@@ -1,8 +1,8 @@
-"""The dense-state gate timer's command line (qsl_gb300/gate_timing.py):
-argument checks that need no GPU."""
+"""The dense-state gate timer's command line (gate_timing.py, beside
+bench.py): argument checks that need no GPU."""
 import pytest
 
-from qsl_gb300 import gate_timing
+import gate_timing
 
 
 def test_rejects_targets_outside_the_state():
@@ -25,3 +25,20 @@ def test_prepare_dense_touches_every_qubit_twice():
     gate_timing.prepare_dense(Rec(), 5)
     assert [c[:2] for c in calls] == [(g, q) for q in range(5) for g in ("rotateY", "rotateZ")]
     assert all(0.3 <= c[2] <= 2.8 for c in calls)
+
+
+def test_rejects_bad_pairs_and_gates():
+    with pytest.raises(SystemExit):
+        gate_timing.main(["--qubits", "10", "--pairs", "3:3"])
+    with pytest.raises(SystemExit):
+        gate_timing.main(["--qubits", "10", "--pairs", "3:10"])
+    with pytest.raises(SystemExit):
+        gate_timing.main(["--qubits", "10", "--gates", "notAGate"])
+
+
+def test_algorithmic_bytes_follow_the_reference_loops():
+    n = 30
+    assert gate_timing.alg_bytes("rotateX", n) == 32 << 30
+    assert gate_timing.alg_bytes("phase", n) == 32 << 29
+    assert gate_timing.alg_bytes("controlNot", n) == 32 << 29
+    assert gate_timing.alg_bytes("controlPhase", n) == 32 << 28

@@ -11,6 +11,7 @@ import os
 import numpy as np
 import pytest
 
+import oracle
 from conftest import bits, random_np_state, random_state
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
@@ -127,7 +128,7 @@ def test_resize_against_reference_fixtures(port, tag):
 
 
 ref_needed = pytest.mark.skipif(
-    not os.path.isdir(os.path.join(os.environ.get("QSL_REFERENCE_SRC", "/root/reference"), "src")),
+    not (oracle.REF_SRC and os.path.isdir(os.path.join(oracle.REF_SRC, "src"))),
     reason="reference source tree absent; the committed fixtures pin the oracle")
 
 

@@ -42,10 +42,41 @@ def test_prob_noalloc_matches_prob_twice(qsl):
                 assert out.value == want, (dtype, n, call, t, o)
 
 
+def test_prob_noalloc_at_its_largest_state(qsl):
+    """27 qubits, the largest state the fixed scratch accepts (the carved
+    scratch and the host arrays are at their fullest), in both dtypes."""
+    torch = pytest.importorskip("torch")
+    L = qsl.lib()
+    rng = np.random.default_rng(27)
+    n = 27
+    for dtype, real, code in ((np.complex128, torch.float64, qsl.C128),
+                              (np.complex64, torch.float32, qsl.C64)):
+        gen = torch.Generator(device="cuda").manual_seed(int(rng.integers(1 << 30)))
+        dev = torch.rand(2 << n, dtype=real, device="cuda", generator=gen) - 0.5
+        dev /= torch.linalg.vector_norm(dev.double()).to(real)
+        ref = qsl.Qubits(n, dtype=dtype)
+        torch.cuda.synchronize()
+        host = dev.cpu().numpy().view(dtype)
+        ref.setState(host)
+        stream = torch.cuda.current_stream().cuda_stream
+        for call in range(2):
+            for t, o in ((0, 0), (13, 1), (26, 0), (26, 1)):
+                want = ref.prob(t, o)
+                out = C.c_double(-1.0)
+                rc = L.qslc_prob_noalloc(dev.data_ptr(), n, code, t, o, stream, C.byref(out))
+                assert rc == 0, L.qslc_last_error()
+                assert out.value == want, (dtype, call, t, o)
+        del ref, dev, host
+        torch.cuda.empty_cache()
+
+
 def test_prob_noalloc_rejects_oversized_states(qsl):
+    """Every qubit count outside [1, 27] is refused before any shift or CUDA
+    call, including counts at and beyond the width of a 64-bit index."""
     L = qsl.lib()
     out = C.c_double()
     dummy = C.c_double(0.0)
-    rc = L.qslc_prob_noalloc(C.addressof(dummy), 28, qsl.C128, 0, 0, None, C.byref(out))
-    assert rc == qsl.EINVAL
-    assert b"27" in L.qslc_last_error()
+    for n in (28, 40, 63, 64, 65, 70, 0):
+        rc = L.qslc_prob_noalloc(C.addressof(dummy), n, qsl.C128, 0, 0, None, C.byref(out))
+        assert rc == qsl.EINVAL, n
+        assert b"27" in L.qslc_last_error(), n
