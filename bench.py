@@ -195,6 +195,15 @@ def run_fused(args, torch, q, stream):
             torch.cuda.empty_cache()
     k = min(by_k, key=lambda kk: by_k[kk]["ms"])
     fused_ms, blocks = by_k[k]["ms"], by_k[k]["blocks"]
+    hbm, hbm_kind = peaks()
+    # one fused block is one sweep of the complex64 state: 2 x 8 B per amplitude
+    block_bytes = 2 * 8 * (1 << n)
+    roof = {"bound": "hbm", "kernel": "k_dense_tc" if k == "5tc" else f"k_dense<{k}>",
+            "alg_bytes_per_launch": block_bytes,
+            "achieved": blocks * block_bytes / (fused_ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+            "peak_source": hbm_kind,
+            "note": "the block sweeps' mean rate over the timed blocks (queue flushes included)"}
+    roof["frac"] = roof["achieved"] / hbm
     su = workloads.uniforms(args.shots, SEED + 5)
     t0 = time.perf_counter()
     sim.sample_shots(su)
@@ -239,7 +248,7 @@ def run_fused(args, torch, q, stream):
             "plain_fp64_gates_per_s_same_size": plain_gps,
             "speedup_vs_plain_fp64": fused_gps / plain_gps,
             "infidelity": 1 - fid, "infidelity_qubits": m, "max_abs_err": maxerr,
-            "sample_shots": args.shots, "sample_ms": sample_ms}
+            "sample_shots": args.shots, "sample_ms": sample_ms, "roofline": roof}
 
 
 def run_np(args, torch, q, stream):
@@ -286,6 +295,61 @@ def run_np(args, torch, q, stream):
 
 
 BATCH_SHOTS = 1024
+SM_COUNT = 152
+
+
+def fp64_peak_gops():
+    """The FP64 pipe's rate: 2 operations per SM per clock (a DFMA probe on
+    GB300 measured 2.07), at the measured maximum SM clock."""
+    mhz = 2070.0
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        mhz = float(json.load(open(p)).get("sm_max_mhz", mhz))
+    return 2 * SM_COUNT * mhz * 1e6 / 1e9
+
+
+def batch_roofline(ns, ls, tile_log2, amp_bytes, kernel_ms, fp64):
+    """Roofline of one batch launch.  HBM: an instance above a shared-memory
+    tile writes its |0..0> state, reads and writes it twice per layer (two
+    passes) and reads it once for the measurements, (2 + 4 L) x 2^n x amp
+    bytes; smaller instances never leave shared memory.  Arithmetic: the
+    FP64 operations the reference's loops perform (12 n 2^n per layer for
+    rotateY and rotateZ on every qubit, 4 n 2^n for the probabilities, 4 x
+    2^n for the CDF), against the FP64 pipe's rate -- the kernel puts part of
+    them on the integer pipes, so this fraction can pass 1."""
+    n = np.asarray(ns, dtype=np.int64)
+    L = np.asarray(ls, dtype=np.int64)
+    big = n > tile_log2
+    hbm_bytes = float(np.sum(np.where(big, (2 + 4 * L) << n, 0)) * amp_bytes)
+    # shared memory: a resident state is read and written by each rotateY
+    # sweep, by the fused rotateZ sweep and by the ladder, per layer
+    smem_bytes = float(np.sum(np.where(big, 0, (L * (n + 2)) << n)) * 2 * amp_bytes)
+    ops = float(np.sum((12 * n * L + 4 * n + 4) << n))
+    sec = kernel_ms * 1e-3
+    hbm, kind = peaks()
+    mhz = fp64_peak_gops() / (2 * SM_COUNT) * 1e3
+    smem_peak = 128 * SM_COUNT * mhz * 1e6 / 1e9
+    out = {"hbm": {"alg_bytes": hbm_bytes, "achieved": hbm_bytes / sec / 1e9, "peak": hbm,
+                   "unit": "GB/s", "peak_source": kind},
+           "smem": {"alg_bytes": smem_bytes, "achieved": smem_bytes / sec / 1e9, "peak": smem_peak,
+                    "unit": "GB/s", "peak_source": "128 B per SM per clock at the measured maximum SM clock"},
+           "instances_in_hbm": int(big.sum())}
+    for k in ("hbm", "smem"):
+        out[k]["frac"] = out[k]["achieved"] / out[k]["peak"]
+    if fp64:
+        peak = fp64_peak_gops()
+        out["fp64"] = {"reference_ops": ops, "achieved": ops / sec / 1e9, "peak": peak,
+                       "unit": "Gop/s", "peak_source": "2 FP64 operations per SM per clock at the "
+                                                        "measured maximum SM clock"}
+    else:
+        peak = 128 * SM_COUNT * mhz * 1e6 / 1e9
+        out["fp32"] = {"reference_ops": ops, "achieved": ops / sec / 1e9, "peak": peak,
+                       "unit": "Gop/s", "peak_source": "128 FP32 operations per SM per clock at the "
+                                                        "measured maximum SM clock"}
+    arith = "fp64" if fp64 else "fp32"
+    out[arith]["frac"] = out[arith]["achieved"] / peak
+    out["bound"] = max(("hbm", "smem", arith), key=lambda k: out[k]["frac"])
+    return out
 
 
 def batch_workload(args):
@@ -323,8 +387,11 @@ def run_batch(args, torch, q):
         for _ in range(reps):
             b.run(angles, u)
         dt_s = (time.perf_counter() - t0) / reps
+        shape = b.shape()
         out[name] = {"s": dt_s, "gates_per_s": total_gates / dt_s, "kernel_ms": tuned_ms,
-                     "shape": b.shape()}
+                     "shape": shape,
+                     "roofline": batch_roofline(ns, ls, shape["tile_log2"], 16 if name == "c128" else 8,
+                                                tuned_ms, name == "c128")}
         del b
     # plain FP64 path on a random subset, scaled by gate count
     sub = rng.choice(ninst, args.batch_plain_sample, replace=False)

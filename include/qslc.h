@@ -228,6 +228,16 @@ QSLC_API int qslc_synchronize(qslc_state *s);
 /* Kernels launched through this handle since it was created. */
 QSLC_API uint64_t qslc_launch_count(const qslc_state *s);
 
+/* No counterpart in the reference (its getState returns a copy,
+ * default.hpp:165): the device address of the stored amplitudes, for
+ * zero-copy interop (a framework tensor over the state, a device-side
+ * comparison).  There are qslc_num_stored amplitudes of 16 (QSLC_C128) or 8
+ * (QSLC_C64) bytes; queued precision-form gates are applied first.  The
+ * address changes when a call reallocates the state (setNumOnes, addQubit,
+ * reallocate, assignment between sizes); work on it must be ordered after
+ * the handle's stream. */
+QSLC_API int qslc_device_amps(qslc_state *s, void **out);
+
 /* Precision form (no counterpart in the reference).  With max_qubits in
  * 1..5 on a complex64 plain state, gates are queued and, at the next call
  * that reads or measures the state (or qslc_flush), fused into dense

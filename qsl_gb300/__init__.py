@@ -68,6 +68,7 @@ SIGNATURES = {
     "qslc_get_stream": (C.c_void_p, [_VP]),
     "qslc_synchronize": (C.c_int, [_VP]),
     "qslc_launch_count": (C.c_uint64, [_VP]),
+    "qslc_device_amps": (C.c_int, [_VP, C.POINTER(C.c_void_p)]),
     "qslc_prob_noalloc": (C.c_int, [_VP, C.c_uint, C.c_int, C.c_uint, C.c_uint, _VP,
                                     C.POINTER(C.c_double)]),
     "qslc_set_fusion": (C.c_int, [_VP, C.c_uint]),
@@ -231,6 +232,32 @@ class Qubits:
 
     def launches(self) -> int:
         return int(self.L.qslc_launch_count(self.h))
+
+    def device_amps(self) -> int:
+        """Device address of the stored amplitudes (qslc_device_amps)."""
+        p = C.c_void_p()
+        _check(self.L.qslc_device_amps(self.h, C.byref(p)))
+        return int(p.value or 0)
+
+    def num_stored(self) -> int:
+        return int(self.L.qslc_num_stored(self.h))
+
+    def device_view(self):
+        """A torch tensor over the stored amplitudes, without a copy: shape
+        (num_stored, 2), float64 or float32 {re, im} pairs.  Valid while the
+        state is not reallocated; order work on it after ``synchronize()``."""
+        import torch
+
+        class _CAI:
+            pass
+        real = "<f8" if self.code == C128 else "<f4"
+        holder = _CAI()
+        holder.__cuda_array_interface__ = {
+            "shape": (self.num_stored(), 2), "typestr": real,
+            "data": (self.device_amps(), False), "version": 3, "strides": None}
+        t = torch.as_tensor(holder, device="cuda")
+        t._qsl_owner = self          # keeps the state alive while the view is
+        return t
 
     def set_stream(self, stream_ptr: int | None) -> None:
         _check(self.L.qslc_set_stream(self.h, stream_ptr))

@@ -7,7 +7,11 @@
 // index there is undefined behaviour, here it is QSLC_EINVAL.
 #include "qslc_internal.cuh"
 
+#include <nvtx3/nvToolsExt.h>
+
+#include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -33,6 +37,53 @@ int cuda_fail(cudaError_t e, const char *what)
         return QSLC_EOOM;
     }
     return QSLC_ECUDA;
+}
+
+NvtxRange::NvtxRange(const char *name) { nvtxRangePushA(name); }
+NvtxRange::~NvtxRange() { nvtxRangePop(); }
+
+namespace {
+
+struct ForcedError {
+    std::string entry;          // entry point name, or "*"
+    int code = 0;               // 0: nothing forced
+    long long after = 0;        // calls that succeed first
+    std::atomic<long long> seen{0};
+
+    ForcedError()
+    {
+        const char *e = std::getenv("QSLC_FORCE_ERROR");
+        if (!e || !*e) return;
+        std::string v(e);
+        const size_t c1 = v.find(':');
+        entry = v.substr(0, c1);
+        code = QSLC_ECUDA;
+        if (c1 != std::string::npos) {
+            const size_t c2 = v.find(':', c1 + 1);
+            code = std::atoi(v.substr(c1 + 1, c2 == std::string::npos ? std::string::npos : c2 - c1 - 1).c_str());
+            if (c2 != std::string::npos) after = std::atoll(v.c_str() + c2 + 1);
+        }
+        if (code <= 0) code = QSLC_ECUDA;
+    }
+};
+
+ForcedError &forced()
+{
+    static ForcedError f;
+    return f;
+}
+
+const int forced_init = (forced(), 0);   // read the variable when the library loads
+
+}  // namespace
+
+int forced_error(const char *name)
+{
+    ForcedError &f = forced();
+    if (!f.code || (f.entry != "*" && f.entry != name)) return 0;
+    if (f.seen.fetch_add(1) < f.after) return 0;
+    g_err = std::string("forced failure of ") + name + " (QSLC_FORCE_ERROR)";
+    return f.code;
 }
 
 unsigned sm_count()
@@ -228,6 +279,7 @@ const char *qslc_last_error(void) { return g_err.c_str(); }
 
 int qslc_create(unsigned nqubits, int dtype, qslc_state **out)
 {
+    QSLC_ENTRY("qslc_create");
     int rc = new_state(nqubits, dtype, out);
     if (rc) return rc;
     qslc_state *s = *out;
@@ -242,6 +294,7 @@ int qslc_create(unsigned nqubits, int dtype, qslc_state **out)
 
 int qslc_create_np(unsigned nqubits, unsigned nones, int dtype, qslc_state **out)
 {
+    QSLC_ENTRY("qslc_create_np");
     if (nqubits > 32)
         return fail(QSLC_EINVAL, "number-preserving states support at most 32 qubits");
     if (nones < 1 || nones >= nqubits)
@@ -267,6 +320,7 @@ int qslc_destroy(qslc_state *s)
 
 int qslc_clone(const qslc_state *src, qslc_state **out)
 {
+    QSLC_ENTRY("qslc_clone");
     int rc = check_handle(src);
     if (!rc) rc = flushed(const_cast<qslc_state *>(src));
     if (rc) return rc;
@@ -296,6 +350,7 @@ int qslc_clone(const qslc_state *src, qslc_state **out)
 
 int qslc_assign(qslc_state *dst, const qslc_state *src)
 {
+    QSLC_ENTRY("qslc_assign");
     int rc = check_handle(dst);
     if (!rc) rc = check_handle(src);
     if (rc) return rc;
@@ -332,6 +387,7 @@ uint64_t qslc_num_stored(const qslc_state *s) { return s ? s->namps : 0; }
 
 int qslc_num_ones(const qslc_state *s, unsigned *out)
 {
+    QSLC_ENTRY("qslc_num_ones");
     int rc = check_handle(s);
     if (rc) return rc;
     if (!s->np) return fail(QSLC_EINVAL, "not a number-preserving state");
@@ -341,6 +397,7 @@ int qslc_num_ones(const qslc_state *s, unsigned *out)
 
 int qslc_set_num_ones(qslc_state *s, unsigned nones)
 {
+    QSLC_ENTRY("qslc_set_num_ones");
     int rc = check_handle(s);
     if (rc) return rc;
     if (!s->np) return fail(QSLC_EINVAL, "not a number-preserving state");
@@ -351,6 +408,7 @@ int qslc_set_num_ones(qslc_state *s, unsigned nones)
 
 int qslc_reset(qslc_state *s)
 {
+    QSLC_ENTRY("qslc_reset");
     int rc = check_handle(s);
     if (rc) return rc;
     s->fuse_queue.clear();
@@ -359,6 +417,7 @@ int qslc_reset(qslc_state *s)
 
 int qslc_set_state(qslc_state *s, const void *amps, uint64_t n_amps)
 {
+    QSLC_ENTRY("qslc_set_state");
     int rc = check_handle(s);
     if (rc) return rc;
     uint64_t dim = uint64_t(1) << s->n;
@@ -392,6 +451,7 @@ int qslc_set_state(qslc_state *s, const void *amps, uint64_t n_amps)
 
 int qslc_get_state(const qslc_state *cs, void *amps, uint64_t n_amps)
 {
+    QSLC_ENTRY("qslc_get_state");
     int rc = check_handle(cs);
     if (rc) return rc;
     qslc_state *s = const_cast<qslc_state *>(cs);
@@ -408,6 +468,7 @@ int qslc_get_state(const qslc_state *cs, void *amps, uint64_t n_amps)
 
 int qslc_set_basis(qslc_state *s, uint64_t index)
 {
+    QSLC_ENTRY("qslc_set_basis");
     int rc = check_handle(s);
     if (rc) return rc;
     if (s->n < 64 && index >= (uint64_t(1) << s->n))
@@ -424,6 +485,7 @@ int qslc_set_basis(qslc_state *s, uint64_t index)
 
 int qslc_gate1(qslc_state *s, int gate, unsigned targ, double angle)
 {
+    QSLC_ENTRY("qslc_gate1");
     int rc = check_handle(s);
     if (!rc) rc = check_q(s, targ);
     if (rc) return rc;
@@ -444,6 +506,7 @@ int qslc_gate1(qslc_state *s, int gate, unsigned targ, double angle)
 
 int qslc_gate2(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle)
 {
+    QSLC_ENTRY("qslc_gate2");
     int rc = check_handle(s);
     if (!rc) rc = check_q(s, q1);
     if (!rc) rc = check_q(s, q2);
@@ -466,6 +529,7 @@ int qslc_gate2(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle)
 
 int qslc_prob(qslc_state *s, unsigned targ, unsigned outcome, double *out)
 {
+    QSLC_ENTRY("qslc_prob");
     int rc = check_handle(s);
     if (!rc) rc = check_q(s, targ);
     if (rc) return rc;
@@ -478,6 +542,7 @@ int qslc_prob(qslc_state *s, unsigned targ, unsigned outcome, double *out)
 
 int qslc_collapse(qslc_state *s, unsigned targ, unsigned outcome, double factor)
 {
+    QSLC_ENTRY("qslc_collapse");
     int rc = check_handle(s);
     if (!rc) rc = check_q(s, targ);
     if (rc) return rc;
@@ -491,6 +556,7 @@ int qslc_collapse(qslc_state *s, unsigned targ, unsigned outcome, double factor)
 
 int qslc_measure(qslc_state *s, unsigned targ, double u, int *outcome)
 {
+    QSLC_ENTRY("qslc_measure");
     double p0;
     int rc = qslc_prob(s, targ, 0, &p0);
     if (rc) return rc;
@@ -506,6 +572,7 @@ int qslc_measure(qslc_state *s, unsigned targ, double u, int *outcome)
 
 int qslc_postselect(qslc_state *s, unsigned targ, unsigned outcome, double *prob)
 {
+    QSLC_ENTRY("qslc_postselect");
     double p;
     int rc = qslc_prob(s, targ, outcome, &p);
     if (rc) return rc;
@@ -522,6 +589,7 @@ int qslc_postselect(qslc_state *s, unsigned targ, unsigned outcome, double *prob
 
 int qslc_create_resizable(unsigned nqubits, int dtype, qslc_state **out)
 {
+    QSLC_ENTRY("qslc_create_resizable");
     int rc = qslc_create(nqubits, dtype, out);
     if (!rc) (*out)->resizable = 1;
     return rc;
@@ -540,6 +608,7 @@ static int check_resizable(const qslc_state *s)
 
 int qslc_add_qubit(qslc_state *s, unsigned targ)
 {
+    QSLC_ENTRY("qslc_add_qubit");
     int rc = check_resizable(s);
     if (rc) return rc;
     if (targ > s->n)
@@ -554,6 +623,7 @@ int qslc_add_qubit(qslc_state *s, unsigned targ)
 
 int qslc_collapse_out(qslc_state *s, unsigned targ, unsigned outcome, double factor)
 {
+    QSLC_ENTRY("qslc_collapse_out");
     int rc = check_resizable(s);
     if (!rc) rc = check_q(s, targ);
     if (rc) return rc;
@@ -566,6 +636,7 @@ int qslc_collapse_out(qslc_state *s, unsigned targ, unsigned outcome, double fac
 
 int qslc_measure_out(qslc_state *s, unsigned targ, double u, int *outcome)
 {
+    QSLC_ENTRY("qslc_measure_out");
     int rc = check_resizable(s);
     if (rc) return rc;
     if (s->n < 2) return fail(QSLC_EINVAL, "cannot remove the last qubit");
@@ -584,6 +655,7 @@ int qslc_measure_out(qslc_state *s, unsigned targ, double u, int *outcome)
 
 int qslc_postselect_out(qslc_state *s, unsigned targ, unsigned outcome, double *prob)
 {
+    QSLC_ENTRY("qslc_postselect_out");
     int rc = check_resizable(s);
     if (rc) return rc;
     if (s->n < 2) return fail(QSLC_EINVAL, "cannot remove the last qubit");
@@ -601,6 +673,7 @@ int qslc_postselect_out(qslc_state *s, unsigned targ, unsigned outcome, double *
 
 int qslc_reallocate(qslc_state *s)
 {
+    QSLC_ENTRY("qslc_reallocate");
     int rc = check_resizable(s);
     if (!rc) rc = flushed(s);
     if (rc) return rc;
@@ -609,6 +682,7 @@ int qslc_reallocate(qslc_state *s)
 
 int qslc_sample(qslc_state *s, unsigned targ, const double *u, uint64_t nshots, uint64_t counts[2])
 {
+    QSLC_ENTRY("qslc_sample");
     if (!counts || (!u && nshots)) return fail(QSLC_EINVAL, "null pointer");
     double p0;
     int rc = qslc_prob(s, targ, 0, &p0);
@@ -623,6 +697,7 @@ int qslc_sample(qslc_state *s, unsigned targ, const double *u, uint64_t nshots, 
 
 int qslc_sample_all(qslc_state *s, const double *u, uint64_t nshots, uint64_t *out)
 {
+    QSLC_ENTRY("qslc_sample_all");
     int rc = check_handle(s);
     if (rc) return rc;
     if (nshots == 0) return QSLC_OK;
@@ -641,6 +716,7 @@ int qslc_sample_all(qslc_state *s, const double *u, uint64_t nshots, uint64_t *o
 
 int qslc_sample_all2(qslc_state *s, const double *u, uint64_t nshots, uint64_t *out)
 {
+    QSLC_ENTRY("qslc_sample_all2");
     int rc = check_handle(s);
     if (rc) return rc;
     if (nshots == 0) return QSLC_OK;
@@ -660,6 +736,7 @@ int qslc_sample_all2(qslc_state *s, const double *u, uint64_t nshots, uint64_t *
 
 int qslc_measure_all(qslc_state *s, double u, uint64_t *outcome)
 {
+    QSLC_ENTRY("qslc_measure_all");
     uint64_t o = 0;
     int rc = qslc_sample_all(s, &u, 1, &o);
     if (rc) return rc;
@@ -671,6 +748,7 @@ int qslc_measure_all(qslc_state *s, double u, uint64_t *outcome)
 
 int qslc_set_stream(qslc_state *s, void *stream)
 {
+    QSLC_ENTRY("qslc_set_stream");
     int rc = check_handle(s);
     if (!rc) rc = flushed(s);
     if (rc) return rc;
@@ -692,6 +770,7 @@ void *qslc_get_stream(const qslc_state *s) { return s ? static_cast<void *>(s->s
 
 int qslc_synchronize(qslc_state *s)
 {
+    QSLC_ENTRY("qslc_synchronize");
     int rc = check_handle(s);
     if (!rc) rc = flushed(s);
     if (rc) return rc;
@@ -701,8 +780,21 @@ int qslc_synchronize(qslc_state *s)
 
 uint64_t qslc_launch_count(const qslc_state *s) { return s ? s->launches : 0; }
 
+int qslc_device_amps(qslc_state *s, void **out)
+{
+    QSLC_ENTRY("qslc_device_amps");
+    int rc = check_handle(s);
+    if (rc) return rc;
+    if (!out) return fail(QSLC_EINVAL, "null output pointer");
+    rc = flushed(s);
+    if (rc) return rc;
+    *out = s->amps;
+    return QSLC_OK;
+}
+
 int qslc_set_fusion(qslc_state *s, unsigned max_qubits)
 {
+    QSLC_ENTRY("qslc_set_fusion");
     int rc = check_handle(s);
     if (rc) return rc;
     if (max_qubits > 5) return fail(QSLC_EINVAL, "fusion blocks span at most 5 qubits");
@@ -716,6 +808,7 @@ int qslc_set_fusion(qslc_state *s, unsigned max_qubits)
 
 int qslc_set_fusion_tc(qslc_state *s, int on)
 {
+    QSLC_ENTRY("qslc_set_fusion_tc");
     int rc = check_handle(s);
     if (!rc) rc = flushed(s);
     if (rc) return rc;
@@ -725,6 +818,7 @@ int qslc_set_fusion_tc(qslc_state *s, int on)
 
 int qslc_flush(qslc_state *s)
 {
+    QSLC_ENTRY("qslc_flush");
     int rc = check_handle(s);
     if (rc) return rc;
     return flushed(s);

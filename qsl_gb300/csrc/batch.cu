@@ -42,20 +42,19 @@ namespace qslc {
 namespace {
 
 constexpr int MAX_Q = 26;
-// Share of the rotation outputs on the integer pipes (complex128), cycled
-// over a thread's successive pairs: two of four, two of four, one of four;
-// and for rotateZ one of two on every qubit (measured on GB300 for 4096
-// instances: 3.29 s of kernel time against 3.49 s with one of two on two
-// qubits of three).  The build can set others (-DQSLC_BATCH_PAT_RY=...,
-// -DQSLC_BATCH_PAT_RZ=...) for tuning.
-#ifndef QSLC_BATCH_PAT_RY
-#define QSLC_BATCH_PAT_RY 0x155u
+// How the rotation outputs are computed (complex128), as mode masks
+// (gatemath.cuh, OutMode): rotateY cycles over a thread's successive pairs
+// through three 8-bit masks, rotateZ over the qubits through three (2 bits
+// per output).  The build can set others (-DQSLC_BATCH_MODES_RY=...,
+// -DQSLC_BATCH_MODES_RZ=...) for tuning.
+#ifndef QSLC_BATCH_MODES_RY
+#define QSLC_BATCH_MODES_RY 0x151515u
 #endif
-#ifndef QSLC_BATCH_PAT_RZ
-#define QSLC_BATCH_PAT_RZ 0x111u
+#ifndef QSLC_BATCH_MODES_RZ
+#define QSLC_BATCH_MODES_RZ 0x090909u
 #endif
-constexpr unsigned BATCH_PAT_RY = QSLC_BATCH_PAT_RY;
-constexpr unsigned BATCH_PAT_RZ = QSLC_BATCH_PAT_RZ;
+constexpr unsigned BATCH_MODES_RY = QSLC_BATCH_MODES_RY;
+constexpr unsigned BATCH_MODES_RZ = QSLC_BATCH_MODES_RZ;
 
 struct InstDesc {
     uint32_t n, L;
@@ -103,6 +102,8 @@ __device__ __forceinline__ Coef<T> dev_coef(T c, T s)
     k.s = s;
     k.kc = emu::make_const(double(c));
     k.ks = emu::make_const(double(s));
+    k.mc = emu::make_mulk(double(c));
+    k.ms = emu::make_mulk(double(s));
     return k;
 }
 
@@ -118,7 +119,7 @@ __device__ __forceinline__ void stage_layer(LayerCoefs<T> &lc, const T *cf, uint
 }
 
 // rotateY on qubit `bit` of a state or tile held at `st` (2^m amplitudes),
-// gates.cpp:169-174; every thread's pairs cycle through BATCH_PAT_RY.
+// gates.cpp:169-174; every thread's pairs cycle through BATCH_MODES_RY.
 template <class T>
 __device__ __forceinline__ void ry_sweep(cplx<T> *st, unsigned m, unsigned bit, const Coef<T> &k)
 {
@@ -127,7 +128,7 @@ __device__ __forceinline__ void ry_sweep(cplx<T> *st, unsigned m, unsigned bit, 
     for (uint64_t j = threadIdx.x; j < half; j += blockDim.x, it = (it == 2 ? 0 : it + 1)) {
         const uint64_t i0 = insert0(j, bit);
         cplx<T> a0 = st[i0], a1 = st[i0 | b];
-        pair_update<T, P_RY>(a0, a1, k, (BATCH_PAT_RY >> (4 * it)) & 15);
+        pair_update<T, P_RY>(a0, a1, k, (BATCH_MODES_RY >> (8 * it)) & 0xFFu);
         st[i0] = a0;
         st[i0 | b] = a1;
     }
@@ -146,12 +147,18 @@ __device__ __forceinline__ cplx<T> rz_all(cplx<T> a, uint64_t x, uint32_t n, con
         const bool one = (x >> q) & 1;
         const T sg = one ? -k.s : k.s;
         emu::MulConst ksg = k.ks, kneg = k.ks;
-        if (one) ksg.sign ^= emu::SIGN;
-        else kneg.sign ^= emu::SIGN;
-        const unsigned em = (BATCH_PAT_RZ >> (4 * (q % 3))) & 3;
+        emu::MulK msg = k.ms, mneg = k.ms;
+        if (one) {
+            ksg.sign ^= emu::SIGN;
+            msg.sign ^= 0x80000000u;
+        } else {
+            kneg.sign ^= emu::SIGN;
+            mneg.sign ^= 0x80000000u;
+        }
+        const unsigned md = (BATCH_MODES_RZ >> (8 * (q % 3))) & 0xFFu;
         const T re = a.x, im = a.y;
-        a.x = dot2<T, false>((em & 1) != 0, re, k.c, k.kc, im, sg, ksg);
-        a.y = dot2<T, false>((em & 2) != 0, im, k.c, k.kc, re, -sg, kneg);
+        a.x = dot2m<T, false>(mode_of(md, 0), re, k.c, k.kc, k.mc, im, sg, ksg, msg);
+        a.y = dot2m<T, false>(mode_of(md, 1), im, k.c, k.kc, k.mc, re, -sg, kneg, mneg);
     }
     return a;
 }
@@ -578,6 +585,7 @@ std::vector<BatchShape> candidates(const qslc_batch *b)
 extern "C" int qslc_batch_create(int dtype, uint32_t ninst, const uint32_t *nqubits,
                                  const uint32_t *nlayers, uint32_t nshots, qslc_batch **out)
 {
+    QSLC_ENTRY("qslc_batch_create");
     if (!out || !nqubits || !nlayers || ninst == 0) return fail(QSLC_EINVAL, "bad batch arguments");
     *out = nullptr;
     if (dtype != QSLC_C128 && dtype != QSLC_C64) return fail(QSLC_EINVAL, "unknown dtype");
@@ -646,6 +654,7 @@ extern "C" int qslc_batch_create(int dtype, uint32_t ninst, const uint32_t *nqub
 extern "C" int qslc_batch_run(qslc_batch *b, const double *angles, const double *uniforms,
                               double *probs, uint64_t *shots)
 {
+    QSLC_ENTRY("qslc_batch_run");
     if (!b || !angles || !probs || (!uniforms && b->nshots) || (!shots && b->nshots))
         return fail(QSLC_EINVAL, "null pointer");
     std::vector<uint32_t> perm;
@@ -660,6 +669,7 @@ extern "C" int qslc_batch_run(qslc_batch *b, const double *angles, const double 
 extern "C" int qslc_batch_autotune(qslc_batch *b, const double *angles, const double *uniforms,
                                    double *best_ms)
 {
+    QSLC_ENTRY("qslc_batch_autotune");
     if (!b || !angles || (!uniforms && b->nshots)) return fail(QSLC_EINVAL, "null pointer");
     std::vector<uint32_t> perm;
     int rc = upload_any(b, angles, uniforms, perm);
@@ -694,6 +704,7 @@ extern "C" int qslc_batch_autotune(qslc_batch *b, const double *angles, const do
 extern "C" int qslc_batch_set_shape(qslc_batch *b, unsigned threads, unsigned tile_log2,
                                     unsigned ctas_per_sm)
 {
+    QSLC_ENTRY("qslc_batch_set_shape");
     if (!b) return fail(QSLC_EINVAL, "null batch");
     BatchShape s;
     s.threads = threads;
@@ -708,6 +719,7 @@ extern "C" int qslc_batch_set_shape(qslc_batch *b, unsigned threads, unsigned ti
 extern "C" int qslc_batch_shape(const qslc_batch *b, unsigned *threads, unsigned *tile_log2,
                                 unsigned *ctas_per_sm, unsigned *grid)
 {
+    QSLC_ENTRY("qslc_batch_shape");
     if (!b) return fail(QSLC_EINVAL, "null batch");
     if (threads) *threads = b->shape.threads;
     if (tile_log2) *tile_log2 = b->shape.tile_log2;

@@ -534,5 +534,149 @@ QSLC_HD uint64_t dot2_rn(uint64_t a, const MulConst &c, uint64_t b, const MulCon
     return (uint64_t(sx) << 32) | ((uint64_t(uint32_t(E + 1022)) << 52) + mr + inc);
 }
 
+// ---------------------------------------------------------------------------
+// RN(a * c) as packed IEEE bits from 32-bit integer work: the product form
+// of the mixed path, where a gate output RN(RN(a*c) + RN(b*s)) takes its
+// products from the integer pipes and its sum from the FP64 pipe (one FP64
+// operation instead of three).
+//
+// The constant's significand is stored shifted left by 11 (C = mc * 2^11,
+// bit 63 set), so the 128-bit product P = ma * C lies in [2^115, 2^117)
+// and the 53 bits it keeps start at bit 64 (or 63): the significand is the
+// high 64-bit word, or that word and one more bit, and the bits below it are
+// whole 32-bit words.  The four 32 x 32 partial products are
+// multiply-adds whose carries never leave 64 bits (they run on the FMA
+// pipe's IMAD.WIDE); the rest is a handful of 32-bit shifts, logic and
+// adds:
+//   - top = bit 116 of P; a funnel shift by 1 - top brings the significand
+//     to 53 bits and leaves the round bit at bit 31 of `rest`;
+//   - the lowest word is jammed into rest's last bit, so the round-to-
+//     nearest-even increment is the carry out of rest + 0x7FFFFFFF + lsb;
+//   - the significand (hidden bit included) is added to the sign and the
+//     exponent field less one, so the hidden bit -- or a rounding carry to
+//     2^53 -- moves into the exponent by itself.
+// A zero a gives a zero of the product's sign.  Subnormal, infinite or NaN
+// operands, and products whose exponent would leave the normal range, set
+// ok = false; the caller then multiplies on the FP64 pipe.
+// ---------------------------------------------------------------------------
+
+// A multiplier fixed for a whole kernel, decoded for prod_pack.  Only
+// constants with 2^-64 <= |c| < 2 are usable (every rotation and phase
+// coefficient but an exact zero or a sine below 2^-64); the accepted
+// multiplicands then do not depend on the constant -- exponent fields 65 to
+// 2044, whose products with any usable constant are normal even after a
+// rounding carry -- so the two products of one operand share that test.
+struct MulK {
+    uint32_t c0, c1;      // mc * 2^11 = c1:c0
+    uint32_t ehi;         // (e(c) - 1) << 20, two's complement
+    uint32_t sign;        // sign of c in bit 31
+    int usable;           // 0: c outside [2^-64, 2) in magnitude, or not finite
+};
+
+constexpr uint32_t PACK_EF_LO20 = 65u << 20;              // lowest accepted exponent field, << 20
+constexpr uint32_t PACK_EF_SPAN20 = (2044u - 65u) << 20;  // accepted span, << 20
+
+QSLC_HD MulK make_mulk(double c)
+{
+    const MulConst k = make_const(c);
+    MulK r{};
+    const uint64_t C = k.m << 11;
+    r.c0 = uint32_t(C);
+    r.c1 = uint32_t(C >> 32);
+    r.ehi = uint32_t(k.e - 1) << 20;
+    r.sign = uint32_t(k.sign >> 32);
+    // product exponent field ef + e(c) + top (+1 after a rounding carry)
+    // stays in [1, 2046] for ef in [65, 2044] when e(c) is in [-64, 0]
+    const int ef = int((dbits(c) >> 52) & 0x7FF);
+    r.usable = (ef != 0 && ef != 0x7FF && k.e >= -64 && k.e <= 0) ? 1 : 0;
+    return r;
+}
+
+QSLC_HD uint32_t fshl1(uint32_t lo, uint32_t hi, uint32_t s)   // (hi:lo) << s >> 32, s in {0, 1}
+{
+#ifdef __CUDA_ARCH__
+    return __funnelshift_l(lo, hi, s);
+#else
+    return (hi << s) | ((lo >> 31) & s);
+#endif
+}
+
+QSLC_HD uint64_t mulwide(uint32_t a, uint32_t b) { return uint64_t(a) * b; }
+
+// (mh:ml:rest) + k as a 96-bit add, returning the top two words with e
+// added to the top one: one carry chain.
+QSLC_HD void add96(uint32_t mh, uint32_t ml, uint32_t rest, uint32_t k, uint32_t e, uint32_t &hi,
+                   uint32_t &lo)
+{
+#ifdef __CUDA_ARCH__
+    uint32_t junk;
+    asm("add.cc.u32 %0, %3, %4;\n\t"
+        "addc.cc.u32 %1, %5, 0;\n\t"
+        "addc.u32 %2, %6, %7;"
+        : "=r"(junk), "=r"(lo), "=r"(hi)
+        : "r"(rest), "r"(k), "r"(ml), "r"(mh), "r"(e));
+#else
+    const uint64_t t0 = uint64_t(rest) + k;
+    const uint64_t t1 = uint64_t(ml) + (t0 >> 32);
+    lo = uint32_t(t1);
+    hi = mh + e + uint32_t(t1 >> 32);
+#endif
+}
+
+// Per-operand part of prod_pack, shared by the operand's products with
+// different constants.
+struct PackOp {
+    uint32_t alo, a1;     // significand: a1 (hidden bit unless zero) : alo
+    uint32_t efield;      // exponent field, in place (<< 20)
+    uint32_t ahi;         // sign source
+    bool zero;
+};
+
+QSLC_HD PackOp pack_operand(uint64_t abits, bool &ok)
+{
+    PackOp o;
+    o.ahi = uint32_t(abits >> 32);
+    o.alo = uint32_t(abits);
+    o.efield = o.ahi & 0x7FF00000u;
+    o.zero = ((o.ahi & 0x7FFFFFFFu) | o.alo) == 0;
+    ok = ok & (o.zero | ((o.efield - PACK_EF_LO20) <= PACK_EF_SPAN20));
+    o.a1 = (o.ahi & 0x000FFFFFu) | (o.zero ? 0u : 0x00100000u);
+    return o;
+}
+
+QSLC_HD uint64_t prod_pack_op(const PackOp &o, const MulK &k)
+{
+    // P = (a1:alo) * (c1:c0) = w3:w2:w1:w0, in [2^115, 2^117) (0 for a zero)
+    const uint64_t p00 = mulwide(o.alo, k.c0);
+    const uint64_t p01 = mulwide(o.alo, k.c1) + (p00 >> 32);
+    const uint64_t p10 = mulwide(o.a1, k.c0) + uint32_t(p01);
+    const uint64_t p11 = mulwide(o.a1, k.c1) + (p01 >> 32) + (p10 >> 32);
+    const uint32_t w0 = uint32_t(p00), w1 = uint32_t(p10);
+    const uint32_t w2 = uint32_t(p11), w3 = uint32_t(p11 >> 32);
+    const uint32_t top20 = w3 & 0x00100000u;          // bit 116 of P, in place
+    const uint32_t s = (top20 >> 20) ^ 1u;
+    const uint32_t mh = fshl1(w2, w3, s), ml = fshl1(w1, w2, s);
+    // c0 has 11 trailing zeros, so w0 does too: w0 >> 11 is nonzero exactly
+    // when w0 is, and lands below the round bit as the sticky bits
+    const uint32_t rest = (w1 << s) | (w0 >> 11);
+    // round to nearest even: the carry out of rest + 0x7FFFFFFF + lsb
+    const uint32_t kround = 0x7FFFFFFFu + (ml & 1u);
+    const uint32_t sg = (o.ahi ^ k.sign) & 0x80000000u;
+    // exponent field less one (the hidden bit adds it back), sign; a zero
+    // keeps only its sign
+    const uint32_t e = (o.zero ? 0u : o.efield + k.ehi + top20) | sg;
+    uint32_t hi, lo;
+    add96(mh, ml, rest, kround, e, hi, lo);
+    return (uint64_t(hi) << 32) | lo;
+}
+
+// RN(a * c) packed, or ok = false when a or the result is outside the
+// covered range (see MulK); the caller then multiplies on the FP64 pipe.
+QSLC_HD uint64_t prod_pack(uint64_t abits, const MulK &k, bool &ok)
+{
+    const PackOp o = pack_operand(abits, ok);
+    return prod_pack_op(o, k);
+}
+
 }  // namespace emu
 }  // namespace qslc

@@ -43,7 +43,7 @@ __global__ void QSLC_SWEEP_BOUNDS k_pair1(cplx<T> *__restrict__ st, uint64_t npa
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
             if (j + r * stride < npairs) {
-                pair_update<T, OP>(a0[r], a1[r], k, (pt >> (4 * r)) & 15);
+                pair_update<T, OP>(a0[r], a1[r], k, (pt >> (8 * r)) & 0xFFu);
                 st[i0[r]] = a0[r];
                 st[i0[r] | bit] = a1[r];
             }
@@ -70,7 +70,7 @@ __global__ void QSLC_SWEEP_BOUNDS k_diag1(cplx<T> *__restrict__ st, uint64_t cou
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
             if (j + r * stride < count) {
-                diag_update<T, OP>(a[r], k, (pt >> (4 * r)) & 3);
+                diag_update<T, OP>(a[r], k, (pt >> (8 * r)) & 0xFFu);
                 st[i[r]] = a[r];
             }
         }
@@ -107,7 +107,7 @@ __global__ void QSLC_SWEEP_BOUNDS k_pair2(cplx<T> *__restrict__ st, uint64_t nqu
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
             if (j + r * stride < nquads) {
-                pair_update<T, OP>(a0[r], a1[r], k, (pt >> (4 * r)) & 15);
+                pair_update<T, OP>(a0[r], a1[r], k, (pt >> (8 * r)) & 0xFFu);
                 st[x1[r]] = a0[r];
                 st[x2[r]] = a1[r];
                 if constexpr (MODE == 2) {
@@ -140,7 +140,7 @@ __global__ void QSLC_SWEEP_BOUNDS k_diag2(cplx<T> *__restrict__ st, uint64_t nqu
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
             if (j + r * stride < nquads) {
-                diag_update<T, OP>(a[r], k, (pt >> (4 * r)) & 3);
+                diag_update<T, OP>(a[r], k, (pt >> (8 * r)) & 0xFFu);
                 st[i[r]] = a[r];
             }
         }
@@ -212,8 +212,9 @@ int gate1_t(qslc_state *s, int gate, unsigned t, double angle)
     cudaStream_t str = s->stream;
     const bool dp = sizeof(T) == 8;
     const unsigned rot = dp ? pattern_rot() : 0, had = dp ? pattern_h() : 0, dg = dp ? pattern_diag() : 0;
-    auto pair = [&](auto op, unsigned pat, const Coef<T> &k, auto cands) {
+    auto pair = [&](auto op, unsigned pat0, const Coef<T> &k, auto cands) {
         constexpr int OP = decltype(op)::value;
+        const unsigned pat = OP == P_H ? pat0 : pattern_for(k, pat0);
         cands(pat, [&](auto c) {
             with_index(s->n, [&](auto ix) {
                 k_pair1<T, OP, decltype(c)::value, decltype(ix)><<<grid, 256, 0, str>>>(st, half, t, k, pat);
@@ -237,9 +238,10 @@ int gate1_t(qslc_state *s, int gate, unsigned t, double angle)
         break;
     case QSLC_PHASE: {
         const Coef<T> k = full_angle<T>(angle);
-        with_pattern<QSLC_DIAG_PATTERNS>(dg, [&](auto c) {
+        const unsigned pd = pattern_for(k, dg);
+        with_pattern<QSLC_DIAG_PATTERNS>(pd, [&](auto c) {
             with_index(s->n, [&](auto ix) {
-                k_diag1<T, D_PHASE, decltype(c)::value, decltype(ix)><<<grid, 256, 0, str>>>(st, half, t, k, dg);
+                k_diag1<T, D_PHASE, decltype(c)::value, decltype(ix)><<<grid, 256, 0, str>>>(st, half, t, k, pd);
             });
         });
         break;
@@ -263,8 +265,9 @@ int gate2_t(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle)
     const bool dp = sizeof(T) == 8;
     const unsigned rot = dp ? pattern_rot() : 0, had = dp ? pattern_h() : 0, dg = dp ? pattern_diag() : 0;
     // pair kernel with operation OP, mode MODE, pattern pat among candidates
-    auto pair = [&](auto op, auto mode, unsigned pat, const Coef<T> &k, auto cands) {
+    auto pair = [&](auto op, auto mode, unsigned pat0, const Coef<T> &k, auto cands) {
         constexpr int OP = decltype(op)::value, MODE = decltype(mode)::value;
+        const unsigned pat = OP == P_H ? pat0 : pattern_for(k, pat0);
         cands(pat, [&](auto c) {
             with_index(s->n, [&](auto ix) {
                 k_pair2<T, OP, MODE, decltype(c)::value, decltype(ix)><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1, b2,
@@ -272,7 +275,7 @@ int gate2_t(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle)
             });
         });
     };
-    auto rot_c = [](unsigned p, auto f) { with_pattern<QSLC_ROT_PATTERNS>(p, f); };
+    auto rot_c = [](unsigned p, auto f) { with_pattern<QSLC_ROT2_PATTERNS>(p, f); };
     auto h_c = [](unsigned p, auto f) { with_pattern<QSLC_H_PATTERNS>(p, f); };
     auto none = [](unsigned p, auto f) { with_pattern<0u>(p, f); };
     using M0 = std::integral_constant<int, 0>;
@@ -307,10 +310,11 @@ int gate2_t(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle)
         break;
     case QSLC_CONTROL_PHASE: {
         const Coef<T> k = full_angle<T>(angle);
-        with_pattern<QSLC_DIAG_PATTERNS>(dg, [&](auto c) {
+        const unsigned pd = pattern_for(k, dg);
+        with_pattern<QSLC_DIAG_PATTERNS>(pd, [&](auto c) {
             with_index(s->n, [&](auto ix) {
                 k_diag2<T, D_PHASE, decltype(c)::value, decltype(ix)><<<grid, 256, 0, str>>>(st, quads, lo, hi, b1 | b2,
-                                                                                         k, dg);
+                                                                                         k, pd);
             });
         });
         break;

@@ -139,19 +139,19 @@ __global__ void QSLC_SWEEP_BOUNDS k_np_single(cplx<T> *__restrict__ st,
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
             if (j + r * stride >= count) continue;
-            const unsigned em = (pt >> (4 * r)) & 3;
+            const unsigned md = (pt >> (8 * r)) & 0xFFu;
             const T re = a[r].x, im = a[r].y;
             if constexpr (K == NP_NEG1 || K == NP_CZ) {
                 a[r].x = R::mul(re, T(-1));
                 a[r].y = R::mul(im, T(-1));
             } else if constexpr (K == NP_RZ0 || K == NP_CRZ01) {
                 // cos*re + sin*im, cos*im - sin*re
-                a[r].x = dot2<T, false>((em & 1) != 0, re, k.c, k.kc, im, k.s, k.ks);
-                a[r].y = dot2<T, true>((em & 2) != 0, im, k.c, k.kc, re, k.s, k.ks);
+                a[r].x = dot2m<T, false>(mode_of(md, 0), re, k.c, k.kc, k.mc, im, k.s, k.ks, k.ms);
+                a[r].y = dot2m<T, true>(mode_of(md, 1), im, k.c, k.kc, k.mc, re, k.s, k.ks, k.ms);
             } else {
                 // phase * amplitude: cos*re - sin*im, cos*im + sin*re
-                a[r].x = dot2<T, true>((em & 1) != 0, re, k.c, k.kc, im, k.s, k.ks);
-                a[r].y = dot2<T, false>((em & 2) != 0, im, k.c, k.kc, re, k.s, k.ks);
+                a[r].x = dot2m<T, true>(mode_of(md, 0), re, k.c, k.kc, k.mc, im, k.s, k.ks, k.ms);
+                a[r].y = dot2m<T, false>(mode_of(md, 1), im, k.c, k.kc, k.mc, re, k.s, k.ks, k.ms);
             }
             st[slot[r]] = a[r];
         }
@@ -184,28 +184,28 @@ __global__ void QSLC_SWEEP_BOUNDS k_np_pair(cplx<T> *__restrict__ st,
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
             if (j + r * stride >= count) continue;
-            const bool E0 = (pt >> (4 * r)) & 1, E1 = (pt >> (4 * r)) & 2;
-            const bool E2 = (pt >> (4 * r)) & 4, E3 = (pt >> (4 * r)) & 8;
+            const unsigned md = (pt >> (8 * r)) & 0xFFu;
+            const unsigned E0 = mode_of(md, 0), E1 = mode_of(md, 1), E2 = mode_of(md, 2), E3 = mode_of(md, 3);
             const cplx<T> p = a0[r], q = a1[r];
             cplx<T> r0, r1;
             if constexpr (K == NP_SWAP) {
                 r0 = q;
                 r1 = p;
             } else if constexpr (K == NP_RX) {       // :316-321
-                r0.x = dot2<T, false>(E0, p.x, k.c, k.kc, q.y, k.s, k.ks);
-                r0.y = dot2<T, true>(E1, p.y, k.c, k.kc, q.x, k.s, k.ks);
-                r1.x = dot2<T, false>(E2, q.x, k.c, k.kc, p.y, k.s, k.ks);
-                r1.y = dot2<T, true>(E3, q.y, k.c, k.kc, p.x, k.s, k.ks);
+                r0.x = dot2m<T, false>(E0, p.x, k.c, k.kc, k.mc, q.y, k.s, k.ks, k.ms);
+                r0.y = dot2m<T, true>(E1, p.y, k.c, k.kc, k.mc, q.x, k.s, k.ks, k.ms);
+                r1.x = dot2m<T, false>(E2, q.x, k.c, k.kc, k.mc, p.y, k.s, k.ks, k.ms);
+                r1.y = dot2m<T, true>(E3, q.y, k.c, k.kc, k.mc, p.x, k.s, k.ks, k.ms);
             } else if constexpr (K == NP_RY) {       // :366-371
-                r0.x = dot2<T, true>(E0, p.x, k.c, k.kc, q.x, k.s, k.ks);
-                r0.y = dot2<T, true>(E1, p.y, k.c, k.kc, q.y, k.s, k.ks);
-                r1.x = dot2<T, false>(E2, p.x, k.s, k.ks, q.x, k.c, k.kc);
-                r1.y = dot2<T, false>(E3, p.y, k.s, k.ks, q.y, k.c, k.kc);
+                r0.x = dot2m<T, true>(E0, p.x, k.c, k.kc, k.mc, q.x, k.s, k.ks, k.ms);
+                r0.y = dot2m<T, true>(E1, p.y, k.c, k.kc, k.mc, q.y, k.s, k.ks, k.ms);
+                r1.x = dot2m<T, false>(E2, p.x, k.s, k.ks, k.ms, q.x, k.c, k.kc, k.mc);
+                r1.y = dot2m<T, false>(E3, p.y, k.s, k.ks, k.ms, q.y, k.c, k.kc, k.mc);
             } else {                                 // NP_H, :409-412
-                r0.x = hdiv<T, false>(E0, p.x, q.x, k);
-                r0.y = hdiv<T, false>(E1, p.y, q.y, k);
-                r1.x = hdiv<T, true>(E2, p.x, q.x, k);
-                r1.y = hdiv<T, true>(E3, p.y, q.y, k);
+                r0.x = hdiv<T, false>(E0 != MD_F, p.x, q.x, k);
+                r0.y = hdiv<T, false>(E1 != MD_F, p.y, q.y, k);
+                r1.x = hdiv<T, true>(E2 != MD_F, p.x, q.x, k);
+                r1.y = hdiv<T, true>(E3 != MD_F, p.y, q.y, k);
             }
             st[s1[r]] = r0;
             st[s2[r]] = r1;
@@ -367,7 +367,7 @@ static int np_gate_t(qslc_state *s, int gate, unsigned q1, unsigned q2, double a
         constexpr int KIND = decltype(kind_tag)::value;
         const uint64_t cnt = tb->len[ti];
         if (cnt == 0) return;
-        const unsigned pat = sizeof(T) == 8 ? pattern_np_diag() : 0u;
+        const unsigned pat = sizeof(T) == 8 ? pattern_for(k, pattern_np_diag()) : 0u;
         auto go = [&](auto c) {
             k_np_single<T, KIND, decltype(c)::value><<<grid_for(cnt), 256, 0, str>>>(st, tb->tab[ti], cnt, rt,
                                                                                      t1, t2, add, k, pat);
@@ -385,7 +385,7 @@ static int np_gate_t(qslc_state *s, int gate, unsigned q1, unsigned q2, double a
         const unsigned lo = q1 < q2 ? q1 : q2, hi = q1 < q2 ? q2 : q1;
         uint32_t b1 = 1u << q1, b2 = 1u << q2;
         if (KIND == NP_SWAP) { b1 = 1u << lo; b2 = 1u << hi; }   // :259-260
-        const unsigned pat = sizeof(T) != 8 ? 0u : (KIND == NP_H ? pattern_h() : pattern_np_pair());
+        const unsigned pat = sizeof(T) != 8 ? 0u : (KIND == NP_H ? pattern_h() : pattern_for(k, pattern_np_pair()));
         auto go = [&](auto c) {
             k_np_pair<T, KIND, decltype(c)::value><<<grid_for(cnt), 256, 0, str>>>(
                 st, tb->tab[T_N2W1], cnt, rt, lo, hi, b1, b2, k, pat);

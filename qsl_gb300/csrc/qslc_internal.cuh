@@ -34,6 +34,28 @@ int cuda_fail(cudaError_t e, const char *what);
     } while (0)
 
 // ---------------------------------------------------------------------------
+// Entry points: every status-returning C function opens an NVTX range named
+// after itself (visible in Nsight timelines; a no-op with no tool attached)
+// and honours host-side fault injection.  QSLC_FORCE_ERROR=name[:code[:after]]
+// makes the entry point `name` (or every one, for "*") return `code`
+// (default QSLC_ECUDA) once `after` calls of it have succeeded, with a
+// message saying so -- so callers' error paths can be tested without a GPU
+// fault.  It is read once, when the library is loaded.
+// ---------------------------------------------------------------------------
+int forced_error(const char *entry);
+
+struct NvtxRange {
+    explicit NvtxRange(const char *name);
+    ~NvtxRange();
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
+#define QSLC_ENTRY(name)                                              \
+    qslc::NvtxRange qslc_nvtx_range_(name);                           \
+    if (int qslc_forced_ = qslc::forced_error(name)) return qslc_forced_
+
+// ---------------------------------------------------------------------------
 // Round-to-nearest arithmetic with no contraction: qsl's x86-64 build rounds
 // every product and every sum on its own, and so must we to produce the
 // same bits.

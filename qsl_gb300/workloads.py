@@ -86,12 +86,24 @@ def np_gaussian_state(n: int, w: int, seed: int, dtype=np.complex128) -> np.ndar
 
 
 def weight_indices(n: int, w: int) -> np.ndarray:
-    """All n-bit integers with w set bits, ascending."""
-    x = np.arange(1 << n, dtype=np.uint64)
-    pc = np.zeros(x.size, dtype=np.uint8)
-    for b in range(n):
-        pc += ((x >> np.uint64(b)) & np.uint64(1)).astype(np.uint8)
-    return np.nonzero(pc == w)[0].astype(np.int64)
+    """All n-bit integers with w set bits, ascending.  Built bit by bit: the
+    k-bit integers of weight j are those of k-1 bits and weight j, then those
+    of weight j-1 with bit k-1 set, so every list stays sorted; only weights
+    that can still reach w are kept."""
+    if w < 0 or w > n:
+        return np.empty(0, dtype=np.int64)
+    layer = {0: np.zeros(1, dtype=np.int64)}
+    for k in range(1, n + 1):
+        new = {}
+        for j in range(max(0, w - (n - k)), min(k, w) + 1):
+            parts = []
+            if j in layer:
+                parts.append(layer[j])
+            if j - 1 in layer:
+                parts.append(layer[j - 1] + (1 << (k - 1)))
+            new[j] = np.concatenate(parts)
+        layer = new
+    return layer[w]
 
 
 def uniforms(count: int, seed: int) -> np.ndarray:

@@ -323,8 +323,96 @@ int main(int argc, char **argv)
         std::printf("only %ld carry cases\n", carry_cases);
         return 3;
     }
-    std::printf("cases %ld fails %ld declined mul %ld add %ld dot2 %ld\n", N, fails, declined_mul,
-                declined_add, declined_dot);
+    // the packed product of the mixed path, prod_pack: random and few-bit
+    // significands, zeros of both signs, products that round up to a power
+    // of two (with either position of the leading bit), and operands at and
+    // beyond the edges of the normal range, which must decline or be exact
+    long declined_pack = 0, pack_carry = 0;
+    for (long i = 0; i < N; i++) {
+        double c = (i & 15) == 0 ? make(-1022, 1023) : make(-6, 1);
+        double a = (i & 15) == 1 ? make(-1022, 1023) : make(-80, 2);
+        const int kind = int(rng() % 16);
+        if (kind == 0) a = (rng() & 1) ? 0.0 : -0.0;
+        if (kind == 1) {                                            // rounds up to 2^53
+            uint64_t ma;
+            const int top = int(rng() & 1);
+            if (carry_significand(make_const(c).m, top, ma)) {
+                a = std::ldexp(double(ma), int(rng() % 60) - 80) * ((rng() & 1) ? -1.0 : 1.0);
+                pack_carry++;
+            }
+        }
+        if (kind == 2) a = dfrom((rng() & MANT) | (rng() & 1 ? SIGN : 0));   // subnormal
+        if (kind == 3) a = (rng() & 1) ? INFINITY : NAN;
+        if (kind == 4) { a = make(1000, 1023); c = make(20, 1023); }           // overflow side
+        if (kind == 5) { a = make(-1022, -1000); c = make(-60, -1); }           // underflow side
+        if (kind == 6) c = make(-1022, -1000);
+        const MulK k = make_mulk(c);
+        bool ok = k.usable != 0;
+        const uint64_t r = prod_pack(dbits(a), k, ok);
+        volatile double ref = a * c;
+        if (!ok) {
+            if (k.usable && (kind <= 1 || kind >= 7)) declined_pack++;   // amplitude-like operands
+            continue;
+        }
+        if (r != dbits(ref)) {
+            if (fails++ < 10) std::printf("prod_pack %a * %a: got %a want %a\n", a, c, dfrom(r), (double)ref);
+        }
+        // a declined-free product must be normal or zero
+        const int ef = int((r >> 52) & 0x7FF);
+        if (!(ef != 0 && ef != 0x7FF) && (r & ~SIGN) != 0) {
+            if (fails++ < 10) std::printf("prod_pack %a * %a accepted a non-normal result\n", a, c);
+        }
+    }
+    {
+        const double usable[4] = {1.0, -0.5, 0x1p-64, 1.9999999999999998};
+        const double unusable[6] = {0.0, 2.0, 0x1.fffffffffffffp-65, 1e-300, INFINITY, 4.9e-324};
+        for (double c : usable)
+            if (!make_mulk(c).usable) { std::printf("constant %a should be usable\n", c); return 6; }
+        for (double c : unusable)
+            if (make_mulk(c).usable) { std::printf("constant %a should not be usable\n", c); return 6; }
+    }
+    if (pack_carry < N / 100) {
+        std::printf("only %ld prod_pack carry cases\n", pack_carry);
+        return 3;
+    }
+    if (declined_pack > N / 20) {
+        std::printf("prod_pack declined %ld of %ld\n", declined_pack, N);
+        return 2;
+    }
+    // every exponent field of a against a few constants: exact where
+    // accepted, and accepted across the whole range a gate constant allows
+    {
+        const double cs[7] = {0.7071067811865476, -0.3826834323650898, 1.9999999999999998,
+                              0.5, 2.2250738585072014e-300, 0x1p-64, -0x1.fffffffffffffp-65};
+        for (double c : cs) {
+            const MulK k = make_mulk(c);
+            for (int ef = 0; ef <= 0x7FF; ef++) {
+                for (int rep = 0; rep < 64; rep++) {
+                    const double a = dfrom((uint64_t(ef) << 52) | (rng() & MANT) | (rep & 1 ? SIGN : 0));
+                    bool ok = k.usable != 0;
+                    const uint64_t r = prod_pack(dbits(a), k, ok);
+                    volatile double ref = a * c;
+                    const int rf = int((dbits(ref) >> 52) & 0x7FF);
+                    if (ok && r != dbits(ref)) {
+                        if (fails++ < 10)
+                            std::printf("prod_pack edge %a * %a: got %a want %a\n", a, c, dfrom(r), (double)ref);
+                    }
+                    // a usable constant declines only operands whose exponent
+                    // field lies outside [65, 2044] (zeros excepted)
+                    (void)rf;
+                    const bool zero_a = (dbits(a) & ~SIGN) == 0;
+                    if (!ok && k.usable && !zero_a && ef >= 65 && ef <= 2044) {
+                        if (fails++ < 10) std::printf("prod_pack declined %a * %a\n", a, c);
+                    }
+                    if (ok && !zero_a && (ef < 65 || ef > 2044)) {
+                        if (fails++ < 10) std::printf("prod_pack accepted %a * %a\n", a, c);
+                    }
+                }
+            }
+        }
+    }
+    std::printf("cases %ld fails %ld declined mul %ld add %ld dot2 %ld prod_pack %ld (carries %ld)\n", N,
+                fails, declined_mul, declined_add, declined_dot, declined_pack, pack_carry);
     if (fails) return 1;
     // declines must be rare on amplitude-like data
     if (declined_add > N / 100 || declined_dot > N / 50 || declined_div > N / 50) return 2;

@@ -14,53 +14,70 @@
 #include <qsl/verify.hpp>
 #include <qsl/qubits/cuda.hpp>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 
 namespace {
 
 int failures = 0;
 
-void expect(bool ok, const char *what)
+const char *section = "";
+
+// Prints every checker statistic with its bound and verdict, so the log
+// shows what each of qsl's checkers reported for the CUDA backend.
+void expect(bool ok, const char *what, double value, double bound)
 {
-    if (!ok) {
-        std::fprintf(stderr, "FAILED: %s\n", what);
-        ++failures;
-    }
+    std::printf("%-8s %-30s %-28s %.3e (bound %.1e)\n", ok ? "PASS" : "FAIL", section, what, value, bound);
+    if (!ok) ++failures;
 }
+
+// The mean relative error of SampleAllChecker compares two independent
+// samplings of 10^6 shots; it grows with the number of outcomes, and the
+// reference bounds it by 15% only at 8 qubits (basic-tests.cpp:455-456).
+// The bound used here is the larger of 15% and 1.5 times what the same
+// checker reports for the reference's own Default/Omp pair on the same
+// state size (a control with no GPU in it).
+double sample_all_bound = 0.15;
 
 // The statistics every measurement checker reports, with the bounds of
 // src/tests/basic-tests.cpp:425-458.
 template <typename V>
 void measurement_checks(V &verify, double state_tol)
 {
+    auto near = [](double v, double want, double tol, const char *what) {
+        expect(std::abs(v - want) < tol, what, std::abs(v - want), tol);
+    };
     auto prob = verify.template check<qsl::ProbChecker>();
-    expect(std::abs(prob.template mean<double>(1)) < 1e-10, "prob outcome 0 difference");
-    expect(std::abs(prob.template mean<double>(2)) < 1e-10, "prob outcome 1 difference");
+    near(prob.template mean<double>(1), 0, 1e-10, "ProbChecker outcome 0");
+    near(prob.template mean<double>(2), 0, 1e-10, "ProbChecker outcome 1");
 
     auto meas = verify.template check<qsl::MeasureChecker>();
-    expect(std::abs(meas.template mean<double>(1) - 1) < 1e-10, "measure interval overlap");
+    near(meas.template mean<double>(1), 1, 1e-10, "MeasureChecker overlap");
 
     auto post = verify.template check<qsl::PostselectChecker>();
-    expect(std::abs(post.template mean<double>(1)) < 1e-10, "postselect prob 0");
-    expect(std::abs(post.template mean<double>(2)) < 1e-10, "postselect prob 1");
-    expect(std::abs(post.template mean<double>(3)) < state_tol, "postselect state 0");
-    expect(std::abs(post.template mean<double>(4)) < state_tol, "postselect state 1");
+    near(post.template mean<double>(1), 0, 1e-10, "PostselectChecker prob 0");
+    near(post.template mean<double>(2), 0, 1e-10, "PostselectChecker prob 1");
+    near(post.template mean<double>(3), 0, state_tol, "PostselectChecker state 0");
+    near(post.template mean<double>(4), 0, state_tol, "PostselectChecker state 1");
 
     auto sample = verify.template check<qsl::SampleChecker>();
-    expect(std::abs(sample.template mean<double>(1) - 1) < 1e-10, "sample interval overlap");
+    near(sample.template mean<double>(1), 1, 1e-10, "SampleChecker overlap");
 
     auto all = verify.template check<qsl::SampleAllChecker>();
-    expect(std::abs(all.overlap_rate - 1) < 1e-10, "sampleAll interval overlap");
-    expect(std::abs(all.mean_relative_error) < 0.15, "sampleAll relative error");
+    near(all.overlap_rate, 1, 1e-10, "SampleAllChecker overlap");
+    near(all.mean_relative_error, 0, sample_all_bound, "SampleAllChecker rel. error");
 }
 
 template <typename Table>
-void gate_checks(const Table &gates)
+void gate_checks(const Table &gates, const char *checker)
 {
     for (const auto &[gate, table] : gates) {
-        expect(std::abs(table.template mean<double>("distance")) < 1e-9, gate.c_str());
+        const std::string what = std::string(checker) + " " + gate;
+        const double d = std::abs(table.template mean<double>("distance"));
+        expect(d < 1e-9, what.c_str(), d, 1e-9);
     }
 }
 
@@ -77,33 +94,47 @@ int main(int argc, char **argv)
     using CudaNP = qsl::Qubits<qsl::cuda_np_type, double>;
     using Resize = qsl::Qubits<qsl::Type::Resize, double>;
     using CudaResize = qsl::Qubits<qsl::cuda_resize_type, double>;
+    using Omp = qsl::Qubits<qsl::Type::Omp, double>;
+
+    {
+        qsl::Verify<Default, Omp, qsl::DefaultStateGen<double>, qsl::SampleAllChecker> control;
+        control.configureState(nqubits);
+        control.configureChecker<qsl::SampleAllChecker>(1000000, 0.99);
+        const double ctl = control.check<qsl::SampleAllChecker>().mean_relative_error;
+        sample_all_bound = std::max(0.15, 1.5 * std::abs(ctl));
+        std::printf("CONTROL  Default vs Omp                 SampleAllChecker rel. error  %.3e -> bound %.3e\n",
+                    std::abs(ctl), sample_all_bound);
+    }
 
     qsl::Verify<Default, Cuda, qsl::DefaultStateGen<double>, qsl::MeasureChecker,
                 qsl::PostselectChecker, qsl::SampleChecker, qsl::SampleAllChecker,
                 qsl::ProbChecker, qsl::DefaultGateChecker>
         full;
+    section = "Default vs Cuda";
     full.configureState(nqubits);
     full.configureChecker<qsl::SampleAllChecker>(1000000, 0.99);
     measurement_checks(full, 1e-7);
-    gate_checks(full.check<qsl::DefaultGateChecker>());
+    gate_checks(full.check<qsl::DefaultGateChecker>(), "DefaultGateChecker");
 
     qsl::Verify<NP, CudaNP, qsl::NPStateGen<double>, qsl::MeasureChecker,
                 qsl::PostselectChecker, qsl::SampleChecker, qsl::SampleAllChecker,
                 qsl::ProbChecker, qsl::NPGateChecker>
         np;
+    section = "NP vs CudaNP";
     np.configureState(nqubits, nones);
     np.configureChecker<qsl::SampleAllChecker>(1000000, 0.99);
     measurement_checks(np, 1e-10);
-    gate_checks(np.check<qsl::NPGateChecker>());
+    gate_checks(np.check<qsl::NPGateChecker>(), "NPGateChecker");
 
     qsl::Verify<Resize, CudaResize, qsl::DefaultStateGen<double>, qsl::MeasureChecker,
                 qsl::PostselectChecker, qsl::SampleChecker, qsl::SampleAllChecker,
                 qsl::ProbChecker, qsl::DefaultGateChecker>
         resize;
+    section = "Resize vs CudaResize";
     resize.configureState(nqubits);
     resize.configureChecker<qsl::SampleAllChecker>(1000000, 0.99);
     measurement_checks(resize, 1e-10);
-    gate_checks(resize.check<qsl::DefaultGateChecker>());
+    gate_checks(resize.check<qsl::DefaultGateChecker>(), "DefaultGateChecker");
 
     std::printf("%s: %d failed checks\n", failures ? "FAIL" : "OK", failures);
     return failures ? 1 : 0;

@@ -1,11 +1,15 @@
 """Every split of the dense gate arithmetic between the FP64 pipe and the
-integer-pipe binary64 emulation gives the oracle's bits.
+integer pipes gives the oracle's bits.
 
-QSLC_EMU_MASK (rotations) and QSLC_EMU_MASK_H (Hadamard) select which of
-the four outputs of an amplitude pair, and QSLC_EMU_MASK_DIAG which of the
-two outputs of a diagonal update, the integer pipes compute -- one mask per
-item of a sweep iteration ("m" or "m0,m1,m2").  The library reads them
-once per process, so each setting runs in its own process."""
+QSLC_EMU_MASK (rotations), QSLC_EMU_MASK_H (Hadamard) and
+QSLC_EMU_MASK_DIAG (phase, controlPhase) choose, per output of an amplitude
+pair or of a diagonal update and per item of a sweep iteration, how it is
+computed: F (FP64 pipe), P (both products on the integer pipes, the sum on
+the FP64 pipe), Q (one product on the integer pipes) or E (all of it on the
+integer pipes), as letters ("PPPQ,PPPP,FFEE"), or in the older numeric form
+(bit i set: output i in mode E).  The library reads them once per process,
+so each setting runs in its own process.  The settings cover the compiled
+patterns and ones that take the runtime-pattern kernels."""
 import os
 import subprocess
 import sys
@@ -49,9 +53,13 @@ def circuit(rng, n, reps):
 
 @pytest.mark.parametrize("rot,had,diag", [("0", "0", "0"), ("1", "5", "2"), ("3,5,1", "15", "1,0,3"),
                                           ("5,5,1", "0", "1,1,0"), ("7", "3,1,0", "3"),
-                                          ("15", "15", "3"), ("10,12,6", "9", "2,1")])
+                                          ("15", "15", "3"), ("10,12,6", "9", "2,1"),
+                                          ("PPPP", "FFFF", "PP"), ("PPPP,PPPP,PPPQ", "EFFF", "PQ"),
+                                          ("PPPQ", "FFFF", "PQ,PP,PP"), ("PPQQ", "EEFF", "QQ"),
+                                          ("QQQQ,PQEF,FEQP", "FEFE", "QP,EF,FQ"),
+                                          ("EPQF", "EEEE", "EP,QE")])
 def test_every_emulation_split_is_exact(qsl, port, tmp_path, rot, had, diag):
-    rng = np.random.default_rng(len(rot) * 7 + len(diag) + int(had.split(",")[0]))
+    rng = np.random.default_rng(len(rot) * 7 + len(diag) + 3 * len(had))
     n = 12
     st = random_state(rng, n)
     names, q1, q2, ang = circuit(rng, n, 6)
@@ -82,7 +90,8 @@ NP_GATES = ("phase", "rotateZ", "controlPhase", "controlRotateZ", "npRotateX", "
 
 
 @pytest.mark.parametrize("pair,diag,had", [("0", "0", "0"), ("15", "3", "15"), ("5,1,1", "1,0,0", "0"),
-                                           ("6,9,3", "2,3,1", "5")])
+                                           ("6,9,3", "2,3,1", "5"), ("PPPQ", "PQ", "FFFF"),
+                                           ("PPPP", "PP", "EEFF"), ("QQQQ,PQEF,FFPP", "QQ,EP,FF", "FFFF")])
 def test_np_emulation_splits_are_exact(qsl, port, tmp_path, pair, diag, had):
     from conftest import random_np_state
     rng = np.random.default_rng(len(pair) + 3 * len(diag))

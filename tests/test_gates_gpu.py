@@ -88,3 +88,27 @@ def test_invalid_arguments_raise(qsl):
     q2 = qsl.Qubits(5)
     with pytest.raises(qsl.LogicError):
         q.assign(q2)
+
+
+@pytest.mark.parametrize("dtype", [np.complex128, np.complex64])
+def test_edge_angles_match_oracle(qsl, port, dtype):
+    """Angles whose coefficients leave the integer products' range -- an
+    exact zero sine (angle 0, 2 pi), a sine below 2^-64 (1e-30) -- run
+    every output on the FP64 pipe; angles near pi give a cosine near
+    2^-54, inside the range.  All must give the oracle's bits."""
+    rng = np.random.default_rng(99)
+    n = 11
+    st = random_state(rng, n, dtype)
+    gpu = qsl.Qubits(state=st, dtype=dtype)
+    cpu = port.PortQubits(n, fp32=dtype == np.complex64, state=st)
+    angles = (0.0, 2 * np.pi, 1e-30, -1e-30, np.pi, -np.pi, 3 * np.pi, 1e-10, 2.0**-70)
+    for a in angles:
+        for g in ("rotateX", "rotateY", "rotateZ", "phase"):
+            for t in (0, 5, n - 1):
+                gpu.gate(g, t, None, a)
+                cpu.gate(g, t, None, a)
+        for g in ("controlRotateX", "controlRotateY", "controlRotateZ", "controlPhase",
+                  "npRotateX", "npRotateY"):
+            gpu.gate(g, 0, n - 1, a)
+            cpu.gate(g, 0, n - 1, a)
+    assert np.array_equal(bits(gpu.getState()), bits(cpu.state))

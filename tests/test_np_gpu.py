@@ -79,3 +79,21 @@ def test_np_construction_semantics(qsl):
     assert q.getNumOnes() == 3 and q.getState()[0b101010] == 1
     with pytest.raises(qsl.LogicError):
         q.pauliX(0)
+
+
+def test_np_edge_angles_match_oracle(qsl, port):
+    """Number-preserving gates at angles whose coefficients leave the
+    integer products' range (exact zero or tiny sines) and near pi."""
+    rng = np.random.default_rng(7)
+    n, w = 10, 4
+    st = random_np_state(rng, n, w)
+    gpu = qsl.QubitsNP(state=st)
+    cpu = port.PortNPQubits(n, w, state=st)
+    for a in (0.0, 2 * np.pi, 1e-30, np.pi, -np.pi, 2.0**-70):
+        for g in ("phase", "rotateZ"):
+            gpu.gate(g, 3, None, a)
+            cpu.gate(g, 3, None, a)
+        for g in ("controlPhase", "controlRotateZ", "npRotateX", "npRotateY"):
+            gpu.gate(g, 0, n - 1, a)
+            cpu.gate(g, 0, n - 1, a)
+    assert np.array_equal(bits(gpu.getState()), bits(cpu.state))
