@@ -113,6 +113,31 @@ int Scratch::ensure(size_t need)
     return QSLC_OK;
 }
 
+int ensure_wait_err(qslc_state *s)
+{
+    if (s->wait_err) return QSLC_OK;
+    void *p = nullptr;
+    if (cudaMalloc(&p, sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(QSLC_EOOM, "out of device memory for the wait error word");
+    }
+    s->wait_err = static_cast<int *>(p);
+    QSLC_CUDA(cudaMemsetAsync(s->wait_err, 0, sizeof(int), s->stream));
+    return QSLC_OK;
+}
+
+int wait_error(qslc_state *s)
+{
+    if (!s->wait_err_pending || !s->wait_err) return QSLC_OK;
+    s->wait_err_pending = false;
+    int h = 0;
+    QSLC_CUDA(cudaMemcpyAsync(&h, s->wait_err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    QSLC_CUDA(cudaStreamSynchronize(s->stream));
+    if (!h) return QSLC_OK;
+    QSLC_CUDA(cudaMemsetAsync(s->wait_err, 0, sizeof(int), s->stream));
+    return fail(QSLC_ETIMEOUT, "a staged sweep's shared-memory barrier wait ran out; the state is undefined");
+}
+
 void Scratch::release()
 {
     if (ptr) cudaFree(ptr);
@@ -134,11 +159,15 @@ int check_handle(const qslc_state *s)
     return QSLC_OK;
 }
 
-// Apply queued gates of the precision form before the state is read.
+// Apply queued gates of the precision form before the state is read, and
+// report a staged sweep whose barrier wait ran out since the last check.
 int flushed(qslc_state *s)
 {
-    if (!s->fuse_queue.empty()) return fusion_flush(s);
-    return QSLC_OK;
+    if (!s->fuse_queue.empty()) {
+        int rc = fusion_flush(s);
+        if (rc) return rc;
+    }
+    return wait_error(s);
 }
 
 // (Re)allocate the amplitude array for `count` amplitudes.
@@ -193,6 +222,7 @@ void free_state(qslc_state *s)
     if (!s) return;
     if (s->stream) cudaStreamSynchronize(s->stream);
     np_release(s);
+    if (s->wait_err) cudaFree(s->wait_err);
     if (s->amps) cudaFree(s->amps);
     s->scratch.release();
     s->scratch2.release();

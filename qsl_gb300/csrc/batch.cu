@@ -51,7 +51,7 @@ constexpr int MAX_Q = 26;
 #define QSLC_BATCH_MODES_RY 0x151515u
 #endif
 #ifndef QSLC_BATCH_MODES_RZ
-#define QSLC_BATCH_MODES_RZ 0x090909u
+#define QSLC_BATCH_MODES_RZ 0x050505u
 #endif
 constexpr unsigned BATCH_MODES_RY = QSLC_BATCH_MODES_RY;
 constexpr unsigned BATCH_MODES_RZ = QSLC_BATCH_MODES_RZ;

@@ -249,7 +249,7 @@ constexpr unsigned PAT_RUNTIME = 0xFFFFFFFFu;
 #define QSLC_ROT_PATTERNS 0u, 0x959595u, 0xA59595u, 0x159595u, 0x999999u, 0x969696u, 0x151515u, 0xA5A5A5u, 0x033333u
 #endif
 #ifndef QSLC_ROT2_PATTERNS
-#define QSLC_ROT2_PATTERNS 0u, 0x959595u, 0x151515u
+#define QSLC_ROT2_PATTERNS 0u, 0x159595u, 0x959595u
 #endif
 #define QSLC_H_PATTERNS 0u, 0x000003u, 0x000303u
 #ifndef QSLC_DIAG_PATTERNS
@@ -376,7 +376,7 @@ inline unsigned parse_pattern(const char *var, const char *dflt, unsigned output
 }
 inline unsigned pattern_rot()
 {
-    static unsigned p = parse_pattern("QSLC_EMU_MASK", "PPPQ", 4);
+    static unsigned p = parse_pattern("QSLC_EMU_MASK", "PPPQ,PPPQ,PPPF", 4);
     return p;
 }
 inline unsigned pattern_h()
@@ -386,7 +386,7 @@ inline unsigned pattern_h()
 }
 inline unsigned pattern_diag()
 {
-    static unsigned p = parse_pattern("QSLC_EMU_MASK_DIAG", "PQ", 2);
+    static unsigned p = parse_pattern("QSLC_EMU_MASK_DIAG", "PQ,PQ,PP", 2);
     return p;
 }
 // The number-preserving sweeps spend integer work on ranking their indices,

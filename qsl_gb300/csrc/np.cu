@@ -120,13 +120,27 @@ __global__ void QSLC_SWEEP_BOUNDS k_np_single(cplx<T> *__restrict__ st,
     using R = rn<T>;
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
     const unsigned pt = CPAT == PAT_RUNTIME ? pat : CPAT;
-    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < count; j += ITEMS * stride) {
+    // the pattern-table entries of the next iteration are read while this
+    // iteration's amplitudes are in flight, so the two dependent DRAM reads
+    // of an item (its pattern, then its amplitude) overlap across iterations
+    const uint64_t j0 = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    uint32_t xn[ITEMS];
+#pragma unroll
+    for (int r = 0; r < ITEMS; r++) xn[r] = (j0 + r * stride < count) ? tab[j0 + r * stride] : 0u;
+    for (uint64_t j = j0; j < count; j += ITEMS * stride) {
         uint32_t slot[ITEMS];
         cplx<T> a[ITEMS];
+        uint32_t xc[ITEMS];
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++) xc[r] = xn[r];
+        const uint64_t jn = j + ITEMS * stride;
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++)
+            if (jn + r * stride < count) xn[r] = tab[jn + r * stride];
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
             if (j + r * stride < count) {
-                const uint32_t x = tab[j + r * stride];
+                const uint32_t x = xc[r];
                 uint32_t y;
                 if constexpr (K == NP_PHASE1 || K == NP_NEG1 || K == NP_RZ0)
                     y = ins_bit(x, t1, 0) | addbits;
@@ -168,13 +182,25 @@ __global__ void QSLC_SWEEP_BOUNDS k_np_pair(cplx<T> *__restrict__ st,
 {
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
     const unsigned pt = CPAT == PAT_RUNTIME ? pat : CPAT;
-    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < count; j += ITEMS * stride) {
+    // next iteration's pattern-table entries read ahead, as in k_np_single
+    const uint64_t j0 = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    uint32_t xn[ITEMS];
+#pragma unroll
+    for (int r = 0; r < ITEMS; r++) xn[r] = (j0 + r * stride < count) ? tab[j0 + r * stride] : 0u;
+    for (uint64_t j = j0; j < count; j += ITEMS * stride) {
         uint32_t s1[ITEMS], s2[ITEMS];
         cplx<T> a0[ITEMS], a1[ITEMS];
+        uint32_t xc[ITEMS];
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++) xc[r] = xn[r];
+        const uint64_t jn = j + ITEMS * stride;
+#pragma unroll
+        for (int r = 0; r < ITEMS; r++)
+            if (jn + r * stride < count) xn[r] = tab[jn + r * stride];
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
             if (j + r * stride < count) {
-                const uint32_t base = ins00(tab[j + r * stride], lo, hi);
+                const uint32_t base = ins00(xc[r], lo, hi);
                 s1[r] = rank_dev(rt, base | b1);
                 s2[r] = rank_dev(rt, base | b2);
                 a0[r] = st[s1[r]];

@@ -140,6 +140,8 @@ struct qslc_state {
     qslc::Scratch fuse_mats;
     qslc::Scratch fuse_tc_mats;   // packed tensor-core operands, then an error word
     uint64_t fused_blocks = 0;
+    int *wait_err = nullptr;         // device word set by a staged sweep whose barrier wait ran out
+    bool wait_err_pending = false;   // staged sweeps launched since the word was last read
 
     size_t amp_bytes() const { return dtype == QSLC_C128 ? 16 : 8; }
 };
@@ -159,6 +161,11 @@ inline unsigned grid_for(uint64_t work, unsigned threads = 256, unsigned per_sm 
 }
 
 int ensure_pinned(qslc_state *s, size_t bytes);
+
+// The device word staged sweeps set when a barrier wait runs out (allocated
+// on first use, zeroed); wait_error() reads and clears it on the host.
+int ensure_wait_err(qslc_state *s);
+int wait_error(qslc_state *s);
 
 // gates.cu
 int launch_gate1(qslc_state *s, int gate, unsigned targ, double angle);

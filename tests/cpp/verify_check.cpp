@@ -41,6 +41,10 @@ void expect(bool ok, const char *what, double value, double bound)
 // checker reports for the reference's own Default/Omp pair on the same
 // state size (a control with no GPU in it).
 double sample_all_bound = 0.15;
+// MeasureChecker and SampleChecker compare confidence intervals of two
+// independent random streams (one per simulator) per qubit; with qsl's
+// defaults (100 draws, 95%) one qubit in twenty misses by chance.  They run
+// here with 1000 draws and 99.9% intervals, so a miss means a bias.
 
 // The statistics every measurement checker reports, with the bounds of
 // src/tests/basic-tests.cpp:425-458.
@@ -113,6 +117,8 @@ int main(int argc, char **argv)
     section = "Default vs Cuda";
     full.configureState(nqubits);
     full.configureChecker<qsl::SampleAllChecker>(1000000, 0.99);
+    full.configureChecker<qsl::MeasureChecker>(1000, 0.999);
+    full.configureChecker<qsl::SampleChecker>(1000, 0.999);
     measurement_checks(full, 1e-7);
     gate_checks(full.check<qsl::DefaultGateChecker>(), "DefaultGateChecker");
 
@@ -123,6 +129,8 @@ int main(int argc, char **argv)
     section = "NP vs CudaNP";
     np.configureState(nqubits, nones);
     np.configureChecker<qsl::SampleAllChecker>(1000000, 0.99);
+    np.configureChecker<qsl::MeasureChecker>(1000, 0.999);
+    np.configureChecker<qsl::SampleChecker>(1000, 0.999);
     measurement_checks(np, 1e-10);
     gate_checks(np.check<qsl::NPGateChecker>(), "NPGateChecker");
 
@@ -133,6 +141,8 @@ int main(int argc, char **argv)
     section = "Resize vs CudaResize";
     resize.configureState(nqubits);
     resize.configureChecker<qsl::SampleAllChecker>(1000000, 0.99);
+    resize.configureChecker<qsl::MeasureChecker>(1000, 0.999);
+    resize.configureChecker<qsl::SampleChecker>(1000, 0.999);
     measurement_checks(resize, 1e-10);
     gate_checks(resize.check<qsl::DefaultGateChecker>(), "DefaultGateChecker");
 

@@ -115,3 +115,25 @@ def test_np_emulation_splits_are_exact(qsl, port, tmp_path, pair, diag, had):
     for g, a, b, x in zip(names, q1, q2, ang):
         cpu.gate(g, a, None if b < 0 else b, x)
     assert np.array_equal(bits(np.load(out)), bits(cpu.state))
+
+
+@pytest.mark.parametrize("rot,diag", [("PPPQ,PPPQ,PPPF", "PQ,PQ,PP"), ("QQQQ,PQEF,FEQP", "QP,EF,FQ")])
+def test_staged_sweeps_are_exact(qsl, port, tmp_path, rot, diag):
+    """With QSLC_BULK=1 the one-qubit sweeps of 8 to 31 qubits stage their
+    amplitudes through shared memory (bulk copies, mbarriers) instead of
+    the register kernels; they must give the same bits, for low targets
+    (one copied run per tile) and high ones (two runs)."""
+    rng = np.random.default_rng(len(rot) + 5 * len(diag))
+    n = 12
+    st = random_state(rng, n)
+    names, q1, q2, ang = circuit(rng, n, 4)
+    inp, out = str(tmp_path / "in.npz"), str(tmp_path / "out.npy")
+    np.savez(inp, state=st, names=names, q1=q1, q2=q2, ang=ang)
+    env = dict(os.environ, QSLC_BULK="1", QSLC_EMU_MASK=rot, QSLC_EMU_MASK_DIAG=diag)
+    r = subprocess.run([sys.executable, "-c", SCRIPT.format(root=ROOT, inp=inp, out=out)],
+                       env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    cpu = port.PortQubits(n, state=st)
+    for g, a, b, x in zip(names, q1, q2, ang):
+        cpu.gate(str(g), int(a), None if int(b) < 0 else int(b), float(x))
+    assert np.array_equal(bits(np.load(out)), bits(cpu.state))
