@@ -1,0 +1,65 @@
+#!/usr/bin/env python3
+"""Device time of the batching kernel on a sub-batch of the benchmark's
+batching workload (a bench tool beside bench.py).
+
+The benchmark's batch is 4,096 ansatz instances (n uniform in [10, 20], L
+in [4, 16]); this tool runs the instances `--first` of it plus the first
+`--largest` 20-qubit ones, as one batch, `--repeat` times, and prints the
+CUDA-event time of each run.  The first run is the ncu capture target of
+one k_batch launch after a warm-up run (`-s 1 -c 1`):
+
+    python batch_timing.py [--first 12] [--largest 4] [--dtype c128] [--repeat 3]
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+import types
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def sub_batch(first: int, largest: int):
+    """Indices of the chosen instances (ascending) and the sub-batch's
+    qubit counts, layer counts, angles and uniforms."""
+    import bench
+    from qsl_gb300 import batch_shards as bs
+    _, ns, ls, _, angles, u = bench.batch_workload(types.SimpleNamespace(batch_instances=4096))
+    idx = np.unique(np.concatenate([np.arange(first), np.nonzero(ns == ns.max())[0][:largest]]))
+    return idx, bs.select(ns, ls, angles, u, bench.BATCH_SHOTS, idx)
+
+
+def main(argv=None) -> None:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--first", type=int, default=12)
+    ap.add_argument("--largest", type=int, default=4)
+    ap.add_argument("--dtype", choices=["c128", "c64"], default="c128")
+    ap.add_argument("--repeat", type=int, default=3)
+    a = ap.parse_args(argv)
+    if a.first < 0 or a.largest < 0 or a.first + a.largest == 0 or a.first > 4096:
+        ap.error("choose at least one instance, at most 4096 of the first ones")
+    import torch
+
+    import bench
+    import qsl_gb300 as q
+    idx, (sn, sl, sa, su) = sub_batch(a.first, a.largest)
+    b = q.Batch(sn, sl, bench.BATCH_SHOTS, dtype=np.complex128 if a.dtype == "c128" else np.complex64)
+    for _ in range(a.repeat):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        b.run(sa, su)
+        e1.record()
+        torch.cuda.synchronize()
+        print(f"{a.dtype} instances {idx.size} (n = {[int(x) for x in sn]}) shape {b.shape()}: "
+              f"{e0.elapsed_time(e1):.1f} ms", flush=True)
+
+
+if __name__ == "__main__":
+    main()

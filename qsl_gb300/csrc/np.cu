@@ -100,6 +100,16 @@ __host__ __device__ __forceinline__ uint32_t ins00(uint32_t x, unsigned lo, unsi
     return (x & lower_mask) + ((x & mid_mask) << 1) + ((x & upper_mask) << 2);
 }
 
+// Items per thread and grid-stride iteration of the NP sweeps.  Each item
+// waits on two dependent reads (its pattern, then its amplitude), so these
+// sweeps are bound by memory latency rather than arithmetic; two items
+// measured faster than three or four on the 28-qubit weight-14 circuit
+// (6964, 6758 and 6466 gates/s).
+#ifndef QSLC_NP_ITEMS
+#define QSLC_NP_ITEMS 2
+#endif
+constexpr int NP_ITEMS = QSLC_NP_ITEMS;
+
 enum NPKind {
     NP_PHASE1, NP_NEG1, NP_RZ0,                 // one-qubit, single amplitude
     NP_CZ, NP_CPHASE, NP_CRZ01,                 // two-qubit, single amplitude
@@ -107,9 +117,8 @@ enum NPKind {
 };
 
 // Single-amplitude updates (np/gates.cpp:53-55, :77-78, :104-106, :148-149,
-// :183-185, :229-231).  Three items per grid-stride iteration, as in the
-// plain sweeps; `pat` chooses per item which of the two outputs run on the
-// integer pipes (gatemath.cuh).
+// :183-185, :229-231).  NP_ITEMS items per grid-stride iteration; `pat`
+// chooses per item how each of the two outputs is computed (gatemath.cuh).
 template <class T, int K, unsigned CPAT = PAT_RUNTIME>
 __global__ void QSLC_SWEEP_BOUNDS k_np_single(cplx<T> *__restrict__ st,
                                                    const uint32_t *__restrict__ tab, uint64_t count,
@@ -124,21 +133,21 @@ __global__ void QSLC_SWEEP_BOUNDS k_np_single(cplx<T> *__restrict__ st,
     // iteration's amplitudes are in flight, so the two dependent DRAM reads
     // of an item (its pattern, then its amplitude) overlap across iterations
     const uint64_t j0 = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    uint32_t xn[ITEMS];
+    uint32_t xn[NP_ITEMS];
 #pragma unroll
-    for (int r = 0; r < ITEMS; r++) xn[r] = (j0 + r * stride < count) ? tab[j0 + r * stride] : 0u;
-    for (uint64_t j = j0; j < count; j += ITEMS * stride) {
-        uint32_t slot[ITEMS];
-        cplx<T> a[ITEMS];
-        uint32_t xc[ITEMS];
+    for (int r = 0; r < NP_ITEMS; r++) xn[r] = (j0 + r * stride < count) ? tab[j0 + r * stride] : 0u;
+    for (uint64_t j = j0; j < count; j += NP_ITEMS * stride) {
+        uint32_t slot[NP_ITEMS];
+        cplx<T> a[NP_ITEMS];
+        uint32_t xc[NP_ITEMS];
 #pragma unroll
-        for (int r = 0; r < ITEMS; r++) xc[r] = xn[r];
-        const uint64_t jn = j + ITEMS * stride;
+        for (int r = 0; r < NP_ITEMS; r++) xc[r] = xn[r];
+        const uint64_t jn = j + NP_ITEMS * stride;
 #pragma unroll
-        for (int r = 0; r < ITEMS; r++)
+        for (int r = 0; r < NP_ITEMS; r++)
             if (jn + r * stride < count) xn[r] = tab[jn + r * stride];
 #pragma unroll
-        for (int r = 0; r < ITEMS; r++) {
+        for (int r = 0; r < NP_ITEMS; r++) {
             if (j + r * stride < count) {
                 const uint32_t x = xc[r];
                 uint32_t y;
@@ -151,7 +160,7 @@ __global__ void QSLC_SWEEP_BOUNDS k_np_single(cplx<T> *__restrict__ st,
             }
         }
 #pragma unroll
-        for (int r = 0; r < ITEMS; r++) {
+        for (int r = 0; r < NP_ITEMS; r++) {
             if (j + r * stride >= count) continue;
             const unsigned md = (pt >> (8 * r)) & 0xFFu;
             const T re = a[r].x, im = a[r].y;
@@ -184,21 +193,21 @@ __global__ void QSLC_SWEEP_BOUNDS k_np_pair(cplx<T> *__restrict__ st,
     const unsigned pt = CPAT == PAT_RUNTIME ? pat : CPAT;
     // next iteration's pattern-table entries read ahead, as in k_np_single
     const uint64_t j0 = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    uint32_t xn[ITEMS];
+    uint32_t xn[NP_ITEMS];
 #pragma unroll
-    for (int r = 0; r < ITEMS; r++) xn[r] = (j0 + r * stride < count) ? tab[j0 + r * stride] : 0u;
-    for (uint64_t j = j0; j < count; j += ITEMS * stride) {
-        uint32_t s1[ITEMS], s2[ITEMS];
-        cplx<T> a0[ITEMS], a1[ITEMS];
-        uint32_t xc[ITEMS];
+    for (int r = 0; r < NP_ITEMS; r++) xn[r] = (j0 + r * stride < count) ? tab[j0 + r * stride] : 0u;
+    for (uint64_t j = j0; j < count; j += NP_ITEMS * stride) {
+        uint32_t s1[NP_ITEMS], s2[NP_ITEMS];
+        cplx<T> a0[NP_ITEMS], a1[NP_ITEMS];
+        uint32_t xc[NP_ITEMS];
 #pragma unroll
-        for (int r = 0; r < ITEMS; r++) xc[r] = xn[r];
-        const uint64_t jn = j + ITEMS * stride;
+        for (int r = 0; r < NP_ITEMS; r++) xc[r] = xn[r];
+        const uint64_t jn = j + NP_ITEMS * stride;
 #pragma unroll
-        for (int r = 0; r < ITEMS; r++)
+        for (int r = 0; r < NP_ITEMS; r++)
             if (jn + r * stride < count) xn[r] = tab[jn + r * stride];
 #pragma unroll
-        for (int r = 0; r < ITEMS; r++) {
+        for (int r = 0; r < NP_ITEMS; r++) {
             if (j + r * stride < count) {
                 const uint32_t base = ins00(xc[r], lo, hi);
                 s1[r] = rank_dev(rt, base | b1);
@@ -208,7 +217,7 @@ __global__ void QSLC_SWEEP_BOUNDS k_np_pair(cplx<T> *__restrict__ st,
             }
         }
 #pragma unroll
-        for (int r = 0; r < ITEMS; r++) {
+        for (int r = 0; r < NP_ITEMS; r++) {
             if (j + r * stride >= count) continue;
             const unsigned md = (pt >> (8 * r)) & 0xFFu;
             const unsigned E0 = mode_of(md, 0), E1 = mode_of(md, 1), E2 = mode_of(md, 2), E3 = mode_of(md, 3);

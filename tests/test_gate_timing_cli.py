@@ -42,3 +42,19 @@ def test_algorithmic_bytes_follow_the_reference_loops():
     assert gate_timing.alg_bytes("phase", n) == 32 << 29
     assert gate_timing.alg_bytes("controlNot", n) == 32 << 29
     assert gate_timing.alg_bytes("controlPhase", n) == 32 << 28
+
+
+def test_batch_timing_picks_the_bench_instances():
+    """batch_timing.py (beside bench.py) runs a sub-batch of the benchmark's
+    4096 instances: the first ones plus the largest, ascending."""
+    import batch_timing
+    idx, (ns, ls, angles, u) = batch_timing.sub_batch(12, 4)
+    assert list(idx[:12]) == list(range(12)) and idx.size == 16
+    assert np_sorted(idx) and list(ns[-4:]) == [20, 20, 20, 20]
+    assert angles.size == int((2 * ns.astype(int) * ls.astype(int)).sum())
+    with pytest.raises(SystemExit):
+        batch_timing.main(["--first", "0", "--largest", "0"])
+
+
+def np_sorted(a):
+    return all(a[i] < a[i + 1] for i in range(len(a) - 1))
