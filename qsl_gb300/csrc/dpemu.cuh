@@ -571,10 +571,6 @@ struct MulK {
     uint32_t ehi;         // (e(c) - 1) << 20, two's complement
     uint32_t sign;        // sign of c in bit 31
     int usable;           // 0: c outside [2^-64, 2) in magnitude, or not finite
-    // multipliers of the FMA-pipe form of prod_pack (QSLC_PACK_FMA): held
-    // here, not written as literals, so the compiler keeps them as integer
-    // multiply-adds instead of turning them back into shifts and adds
-    uint32_t one, two, neg1, neg2, k12, k21;
 };
 
 constexpr uint32_t PACK_EF_LO20 = 65u << 20;              // lowest accepted exponent field, << 20
@@ -589,12 +585,6 @@ QSLC_HD MulK make_mulk(double c)
     r.c1 = uint32_t(C >> 32);
     r.ehi = uint32_t(k.e - 1) << 20;
     r.sign = uint32_t(k.sign >> 32);
-    r.one = 1u;
-    r.two = 2u;
-    r.neg1 = 0xFFFFFFFFu;
-    r.neg2 = 0xFFFFFFFEu;
-    r.k12 = 1u << 12;
-    r.k21 = 1u << 21;
     // product exponent field ef + e(c) + top (+1 after a rounding carry)
     // stays in [1, 2046] for ef in [65, 2044] when e(c) is in [-64, 0]
     const int ef = int((dbits(c) >> 52) & 0x7FF);
@@ -670,29 +660,6 @@ QSLC_HD uint64_t prod_pack_op(const PackOp &o, const MulK &k)
     // keeps only its sign
     const uint32_t e = (o.zero ? 0u : o.efield + k.ehi + top20) | sg;
     uint32_t hi, lo;
-#if defined(__CUDA_ARCH__) && defined(QSLC_PACK_FMA) && QSLC_PACK_FMA
-    // The same steps as below, with the shifts by s in {0, 1} as multiplies
-    // by 1 + s and the bits shifted in as high halves of multiplies by 2s,
-    // and the rounding add as a multiply-add carry chain: integer work the
-    // FMA pipe takes from the ALU pipe.
-    uint32_t t, m1, m2, mh, ml, x1, rest;
-    asm("mul.hi.u32 %0, %1, %2;" : "=r"(t) : "r"(top20), "r"(k.k12));           // top
-    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(m1) : "r"(t), "r"(k.neg1), "r"(k.two));   // 1 + s
-    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(m2) : "r"(t), "r"(k.neg2), "r"(k.two));   // 2 s
-    asm("{\n\t.reg .u32 h;\n\tmul.hi.u32 h, %1, %2;\n\tmad.lo.u32 %0, %3, %4, h;\n\t}"
-        : "=r"(mh) : "r"(w2), "r"(m2), "r"(w3), "r"(m1));
-    asm("{\n\t.reg .u32 h;\n\tmul.hi.u32 h, %1, %2;\n\tmad.lo.u32 %0, %3, %4, h;\n\t}"
-        : "=r"(ml) : "r"(w1), "r"(m2), "r"(w2), "r"(m1));
-    asm("mul.lo.u32 %0, %1, %2;" : "=r"(x1) : "r"(w1), "r"(m1));
-    asm("mul.hi.u32 %0, %1, %2;" : "=r"(rest) : "r"(w0), "r"(k.k21));          // w0 >> 11
-    rest |= x1;
-    const uint32_t kround = 0x7FFFFFFFu + (ml & 1u);
-    asm("mad.lo.cc.u32 %0, %2, %3, %4;\n\t"
-        "madc.lo.cc.u32 %0, %5, %3, 0;\n\t"
-        "madc.lo.u32 %1, %6, %3, %7;"
-        : "=&r"(lo), "=r"(hi)
-        : "r"(rest), "r"(k.one), "r"(kround), "r"(ml), "r"(mh), "r"(e));
-#else
     const uint32_t s = (top20 >> 20) ^ 1u;
     const uint32_t mh = fshl1(w2, w3, s), ml = fshl1(w1, w2, s);
     // c0 has 11 trailing zeros, so w0 does too: w0 >> 11 is nonzero exactly
@@ -701,7 +668,6 @@ QSLC_HD uint64_t prod_pack_op(const PackOp &o, const MulK &k)
     // round to nearest even: the carry out of rest + 0x7FFFFFFF + lsb
     const uint32_t kround = 0x7FFFFFFFu + (ml & 1u);
     add96(mh, ml, rest, kround, e, hi, lo);
-#endif
     return (uint64_t(hi) << 32) | lo;
 }
 
