@@ -134,6 +134,54 @@ __device__ __forceinline__ void ry_sweep(cplx<T> *st, unsigned m, unsigned bit, 
     }
 }
 
+// rotateY on qubit `b0` and then on qubit `b1` (b0 < b1) of a state or tile
+// at `st`, in one sweep: each thread holds the four amplitudes that differ
+// only in those two bits, applies the first gate to its two pairs and then
+// the second gate to its two pairs.  Every amplitude sees the operations of
+// the two sweeps in their order, so the bits are those of two ry_sweep
+// calls, with one barrier instead of two.
+template <class T>
+__device__ __forceinline__ void ry_sweep2(cplx<T> *st, unsigned m, unsigned b0, unsigned b1, const Coef<T> &k0,
+                                          const Coef<T> &k1)
+{
+    const uint64_t quarter = uint64_t(1) << (m - 2);
+    const uint64_t B0 = uint64_t(1) << b0, B1 = uint64_t(1) << b1;
+    for (uint64_t j = threadIdx.x; j < quarter; j += blockDim.x) {
+        const uint64_t x = insert00(j, b0, b1);
+        cplx<T> a00 = st[x], a01 = st[x | B0], a10 = st[x | B1], a11 = st[x | B0 | B1];
+        pair_update<T, P_RY>(a00, a01, k0, BATCH_MODES_RY & 0xFFu);
+        pair_update<T, P_RY>(a10, a11, k0, (BATCH_MODES_RY >> 8) & 0xFFu);
+        pair_update<T, P_RY>(a00, a10, k1, (BATCH_MODES_RY >> 16) & 0xFFu);
+        pair_update<T, P_RY>(a01, a11, k1, BATCH_MODES_RY & 0xFFu);
+        st[x] = a00;
+        st[x | B0] = a01;
+        st[x | B1] = a10;
+        st[x | B0 | B1] = a11;
+    }
+}
+
+// rotateY on the qubits lo..hi-1 of the circuit, in order, on bits
+// off + (q - lo) of a state or tile of 2^m amplitudes: two gates per sweep
+// (ry_sweep2), the last one alone when their number is odd; a barrier after
+// each sweep.
+#ifndef QSLC_BATCH_RY_PAIRS
+#define QSLC_BATCH_RY_PAIRS 1
+#endif
+template <class T>
+__device__ __forceinline__ void ry_layer(cplx<T> *st, unsigned m, unsigned lo, unsigned hi, unsigned off,
+                                         const LayerCoefs<T> &lc)
+{
+    unsigned q = lo;
+    for (; QSLC_BATCH_RY_PAIRS && q + 1 < hi; q += 2) {
+        ry_sweep2<T>(st, m, off + (q - lo), off + (q + 1 - lo), lc.ry[q], lc.ry[q + 1]);
+        __syncthreads();
+    }
+    for (; q < hi; q++) {
+        ry_sweep<T>(st, m, off + (q - lo), lc.ry[q]);
+        __syncthreads();
+    }
+}
+
 // rotateZ on qubits 0..n-1, in that order, of the amplitude at basis index
 // x (gates.cpp:200-205): the |0> member takes (re*c + im*s, im*c - re*s),
 // the |1> member (re*c - im*s, im*c + re*s).  Both are re*c + im*sg and
@@ -264,10 +312,7 @@ __device__ void run_small(cplx<T> *sm, LayerCoefs<T> &lc, const InstDesc &d, con
     }
     for (uint32_t l = 0; l < d.L; l++) {
         stage_layer<T>(lc, coef + d.coef + uint64_t(l) * n * 4, n);   // also orders the fill
-        for (uint32_t q = 0; q < n; q++) {
-            ry_sweep<T>(sm, n, q, lc.ry[q]);
-            __syncthreads();
-        }
+        ry_layer<T>(sm, n, 0, n, 0, lc);
         for (uint64_t i = tid; i < dim; i += nt) sm[i] = rz_all<T>(sm[i], i, n, lc);
         __syncthreads();
         for (uint32_t q = 0; q + 1 < n; q++) {       // controlNot(q, q+1), gates.cpp:215-240
@@ -309,10 +354,7 @@ __device__ cplx<T> *run_big(cplx<T> *sm, LayerCoefs<T> &lc, const InstDesc &d, c
             cplx<T> *g = src + (t << k);
             for (uint64_t i = tid; i < tile; i += nt) sm[i] = g[i];
             __syncthreads();
-            for (unsigned q = 0; q < k; q++) {
-                ry_sweep<T>(sm, k, q, lc.ry[q]);
-                __syncthreads();
-            }
+            ry_layer<T>(sm, k, 0, k, 0, lc);
             for (uint64_t i = tid; i < tile; i += nt) g[i] = sm[i];
             __syncthreads();
         }
@@ -322,10 +364,7 @@ __device__ cplx<T> *run_big(cplx<T> *sm, LayerCoefs<T> &lc, const InstDesc &d, c
             const uint64_t mid = t << c;
             for (uint64_t i = tid; i < tile; i += nt) sm[i] = src[((i >> c) << k) | mid | (i & cmask)];
             __syncthreads();
-            for (unsigned q = k; q < n; q++) {
-                ry_sweep<T>(sm, k, c + (q - k), lc.ry[q]);
-                __syncthreads();
-            }
+            ry_layer<T>(sm, k, k, n, c, lc);
             // outputs in order of their destination: o = (high bits << c) |
             // (low c bits of y); the source's low bits are the inverse of the
             // ladder on those c bits, so consecutive o land on consecutive y
