@@ -9,6 +9,11 @@ CUDA-event time of each run.  The first run is the ncu capture target of
 one k_batch launch after a warm-up run (`-s 1 -c 1`):
 
     python batch_timing.py [--first 12] [--largest 4] [--dtype c128] [--repeat 3]
+                           [--shape THREADS,TILE_LOG2,CTAS_PER_SM]
+
+Without `--shape` the batch keeps its default launch shape (1024 threads,
+one CTA per SM, the larger tile); the benchmark's autotuner picks among
+the shapes `Batch.shapes()` lists.
 """
 from __future__ import annotations
 
@@ -40,15 +45,26 @@ def main(argv=None) -> None:
     ap.add_argument("--largest", type=int, default=4)
     ap.add_argument("--dtype", choices=["c128", "c64"], default="c128")
     ap.add_argument("--repeat", type=int, default=3)
+    ap.add_argument("--shape", default=None, help="threads,tile_log2,ctas_per_sm")
     a = ap.parse_args(argv)
     if a.first < 0 or a.largest < 0 or a.first + a.largest == 0 or a.first > 4096:
         ap.error("choose at least one instance, at most 4096 of the first ones")
+    shape = None
+    if a.shape is not None:
+        try:
+            shape = tuple(int(v) for v in a.shape.split(","))
+        except ValueError:
+            shape = ()
+        if len(shape) != 3:
+            ap.error("--shape takes three integers: threads,tile_log2,ctas_per_sm")
     import torch
 
     import bench
     import qsl_gb300 as q
     idx, (sn, sl, sa, su) = sub_batch(a.first, a.largest)
     b = q.Batch(sn, sl, bench.BATCH_SHOTS, dtype=np.complex128 if a.dtype == "c128" else np.complex64)
+    if shape is not None:
+        b.set_shape(*shape)
     for _ in range(a.repeat):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)

@@ -54,6 +54,107 @@ __global__ void QSLC_SWEEP_BOUNDS k_pair1(cplx<T> *__restrict__ st, uint64_t npa
     }
 }
 
+// x with its sign bit XORed with bit 31 of `m` (an exact negation when set);
+// integer operations, so a per-lane choice of sign never becomes a branch.
+__device__ __forceinline__ double flip_sign(double x, uint32_t m)
+{
+    return __hiloint2double(__double2hiint(x) ^ int(m), __double2loint(x));
+}
+__device__ __forceinline__ float flip_sign(float x, uint32_t m)
+{
+    return __int_as_float(__float_as_int(x) ^ int(m));
+}
+// x when m is 0, y when m is all ones, by bit operations.
+__device__ __forceinline__ double pick(double x, double y, uint32_t m)
+{
+    const int hi = (__double2hiint(x) & ~int(m)) | (__double2hiint(y) & int(m));
+    const int lo = (__double2loint(x) & ~int(m)) | (__double2loint(y) & int(m));
+    return __hiloint2double(hi, lo);
+}
+__device__ __forceinline__ float pick(float x, float y, uint32_t m)
+{
+    return __int_as_float((__float_as_int(x) & ~int(m)) | (__float_as_int(y) & int(m)));
+}
+
+// One output pair of a one-qubit pair gate, computed by the lane that holds
+// amplitude `a` (side 0: a = a0, side 1: a = a1) from its partner `o`.  Each
+// output is the same RN(p1 +- p2) of the same products as in pair_update:
+// the lane's side is folded into exact sign flips (x - y == x + (-y),
+// RN(-x) == -RN(x)) and the order of a sum's two terms (they commute), so
+// every lane of a warp runs the same instructions.  `m1` is 0x80000000 on
+// side 1 and 0 on side 0, `m0` the opposite.  Modes E0, E1 of `md` apply to
+// the lane's x and y outputs.
+//
+// Hadamard's side 1 takes its difference as a0 + (-a1) with the terms
+// swapped in, not as a negated a1 - a0: the two differ in the sign of an
+// exact zero.
+template <class T, int OP>
+__device__ __forceinline__ void lane_update(cplx<T> &a, const cplx<T> &o, uint32_t m0, uint32_t m1,
+                                            const Coef<T> &k, unsigned md)
+{
+    const unsigned E0 = mode_of(md, 0), E1 = mode_of(md, 1);
+    cplx<T> r;
+    if constexpr (OP == P_SWAP) {
+        r = o;
+    } else if constexpr (OP == P_Y) {        // side 0: (a1.y, -a1.x); side 1: (-a0.y, a0.x)
+        r.x = flip_sign(o.y, m1);
+        r.y = flip_sign(o.x, m0);
+    } else if constexpr (OP == P_H) {        // side 0: (a0 + a1)/r; side 1: (a0 + (-a1))/r
+        const uint32_t all = uint32_t(int32_t(m1) >> 31);
+        r.x = hdiv<T, false>(E0 != MD_F, pick(a.x, o.x, all), flip_sign(pick(o.x, a.x, all), m1), k);
+        r.y = hdiv<T, false>(E1 != MD_F, pick(a.y, o.y, all), flip_sign(pick(o.y, a.y, all), m1), k);
+    } else if constexpr (OP == P_RX) {       // the same on both sides
+        r.x = dot2m<T, false>(E0, a.x, k.c, k.kc, k.mc, o.y, k.s, k.ks, k.ms);
+        r.y = dot2m<T, true>(E1, a.y, k.c, k.kc, k.mc, o.x, k.s, k.ks, k.ms);
+    } else if constexpr (OP == P_RY) {       // side 0: a0 c - a1 s; side 1: a1 c + a0 s
+        r.x = dot2m<T, false>(E0, a.x, k.c, k.kc, k.mc, flip_sign(o.x, m0), k.s, k.ks, k.ms);
+        r.y = dot2m<T, false>(E1, a.y, k.c, k.kc, k.mc, flip_sign(o.y, m0), k.s, k.ks, k.ms);
+    } else {                                 // P_RZ, no partner: side 1 flips the sign of s
+        r.x = dot2m<T, false>(E0, a.x, k.c, k.kc, k.mc, flip_sign(a.y, m1), k.s, k.ks, k.ms);
+        r.y = dot2m<T, true>(E1, a.y, k.c, k.kc, k.mc, flip_sign(a.x, m1), k.s, k.ks, k.ms);
+    }
+    a = r;
+}
+
+// One-qubit pair gates on targets 0-4 as warp exchanges (QSLC_SHFL=1).  A
+// pair (i, i ^ 2^t) then lies within 32 consecutive amplitudes: lane l of a
+// warp holds amplitude base + l, so a warp loads and stores 512 contiguous
+// bytes per item, and takes its partner's amplitude from lane l ^ 2^t with
+// shuffles.  A lane holds 2 ITEMS amplitudes per iteration, the register
+// sweep's ITEMS pairs; item 2r takes modes E0, E1 of the pattern's item r,
+// item 2r + 1 its E2, E3, so the split between the pipes is the same.
+// `namps` is a multiple of 32 and the stride a multiple of the block, so
+// the loop bound and every item test are the same across a warp, and the
+// shuffles always run with all 32 lanes.
+template <class T, int OP, unsigned CPAT = PAT_RUNTIME, class IX = uint64_t>
+__global__ void QSLC_SWEEP_BOUNDS k_pair1_shfl(cplx<T> *__restrict__ st, uint64_t namps, unsigned t,
+                                                Coef<T> k, unsigned pat)
+{
+    constexpr int N = 2 * ITEMS;
+    const IX stride = IX(gridDim.x) * blockDim.x;
+    const unsigned pt = CPAT == PAT_RUNTIME ? pat : CPAT;
+    const unsigned lanebit = 1u << t;
+    const uint32_t m1 = (threadIdx.x & lanebit) ? 0x80000000u : 0u, m0 = m1 ^ 0x80000000u;
+    for (IX i = IX(blockIdx.x) * blockDim.x + threadIdx.x; i < IX(namps); i += N * stride) {
+        cplx<T> a[N];
+#pragma unroll
+        for (int r = 0; r < N; r++)
+            if (i + r * stride < namps) a[r] = st[i + r * stride];
+#pragma unroll
+        for (int r = 0; r < N; r++) {
+            if (i + r * stride < namps) {
+                cplx<T> o = a[r];
+                if constexpr (OP != P_RZ) {
+                    o.x = __shfl_xor_sync(0xFFFFFFFFu, a[r].x, lanebit);
+                    o.y = __shfl_xor_sync(0xFFFFFFFFu, a[r].y, lanebit);
+                }
+                lane_update<T, OP>(a[r], o, m0, m1, k, ((pt >> (8 * (r >> 1))) >> (4 * (r & 1))) & 0xFu);
+                st[i + r * stride] = a[r];
+            }
+        }
+    }
+}
+
 // One-qubit diagonal gates on the |1> half: index insert0(j, t) | 2^t.
 template <class T, int OP, unsigned CPAT = PAT_RUNTIME, class IX = uint64_t>
 __global__ void QSLC_SWEEP_BOUNDS k_diag1(cplx<T> *__restrict__ st, uint64_t count,
@@ -407,6 +508,30 @@ inline bool bulk_enabled()
     return on;
 }
 
+// The warp-exchange sweeps (k_pair1_shfl) take one-qubit pair gates on
+// targets 0-4 of states of at least 5 qubits.  By default only pauliX and
+// pauliY, which move amplitudes without arithmetic: on a dense 28-qubit
+// state they run at 6.64-6.67 TB/s there against 6.16-6.69 for the
+// register sweeps.  The rotations and Hadamard stay on the register sweeps
+// (5.43-5.82 TB/s against 4.89-5.30 exchanged), whose thread computes both
+// outputs of a pair from operands it decodes once.  QSLC_SHFL=1 sends every
+// pair gate on those targets through the exchange, QSLC_SHFL=0 none.
+inline int shfl_mode()
+{
+    static const int m = [] {
+        const char *e = std::getenv("QSLC_SHFL");
+        return e && e[0] == '1' ? 1 : e && e[0] == '0' ? 0 : -1;
+    }();
+    return m;
+}
+
+inline bool use_shfl(int op, unsigned t, unsigned n)
+{
+    if (t >= 5 || n < 5) return false;
+    const int m = shfl_mode();
+    return m == 1 || (m == -1 && (op == P_SWAP || op == P_Y));
+}
+
 template <class T>
 bool use_bulk(const qslc_state *s)
 {
@@ -470,6 +595,13 @@ int gate1_t(qslc_state *s, int gate, unsigned t, double angle)
         constexpr int OP = decltype(op)::value;
         const unsigned pat = OP == P_H ? pat0 : pattern_for(k, pat0);
         cands(pat, [&](auto c) {
+            if (use_shfl(OP, t, s->n)) {
+                with_index(s->n, [&](auto ix) {
+                    k_pair1_shfl<T, OP, decltype(c)::value, decltype(ix)>
+                        <<<grid_for(2 * half), 256, 0, str>>>(st, 2 * half, t, k, pat);
+                });
+                return;
+            }
             if constexpr (sizeof(T) == 8) {
                 if (bulk) {
                     brc = launch_bulk<T>(s, k_pair1_bulk<T, OP, decltype(c)::value>, ntiles, t, k, pat);

@@ -137,3 +137,64 @@ def test_staged_sweeps_are_exact(qsl, port, tmp_path, rot, diag):
     for g, a, b, x in zip(names, q1, q2, ang):
         cpu.gate(str(g), int(a), None if int(b) < 0 else int(b), float(x))
     assert np.array_equal(bits(np.load(out)), bits(cpu.state))
+
+
+SCRIPT_DTYPE = r"""
+import sys, numpy as np
+sys.path.insert(0, {root!r})
+import qsl_gb300 as q
+d = np.load({inp!r})
+sim = q.Qubits(state=d["state"], dtype=d["state"].dtype)
+for g, a, x in zip(d["names"], d["q1"], d["ang"]):
+    sim.gate(str(g), int(a), None, float(x))
+np.save({out!r}, sim.getState())
+"""
+
+PAIR1 = ("pauliX", "pauliY", "hadamard", "rotateX", "rotateY", "rotateZ")
+
+
+def _run_pair1(tmp_path, tag, st, names, q1, ang, env):
+    inp, out = str(tmp_path / f"in_{tag}.npz"), str(tmp_path / f"out_{tag}.npy")
+    np.savez(inp, state=st, names=names, q1=q1, ang=ang)
+    r = subprocess.run([sys.executable, "-c", SCRIPT_DTYPE.format(root=ROOT, inp=inp, out=out)],
+                       env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    return np.load(out)
+
+
+@pytest.mark.parametrize("n", [5, 6, 11])
+@pytest.mark.parametrize("rot,had", [("PPPQ,PPPQ,PPPF", "FFFF"), ("QQQQ,PQEF,FEQP", "FEFE"), ("0", "0")])
+def test_warp_exchange_sweeps_are_exact(qsl, port, tmp_path, n, rot, had):
+    """With QSLC_SHFL=1 the one-qubit pair gates on targets 0-4 take each
+    pair's partner amplitude from another lane of the warp (k_pair1_shfl)
+    instead of loading both members in one thread.  Every target 0-4 and
+    every pair gate, with several splits between the pipes: complex128
+    gives the oracle's bits, complex64 the register sweeps' bits.  A
+    uniform state gives pairs of equal amplitudes, whose Hadamard
+    difference is an exact zero (+0 in the reference)."""
+    rng = np.random.default_rng(100 * n + len(rot) + len(had))
+    names, q1, ang = [], [], []
+    for _ in range(3):
+        for g in PAIR1:
+            for t in rng.permutation(min(n, 6)):
+                names.append(g)
+                q1.append(int(t))
+                ang.append(float(rng.uniform(0, 2 * np.pi)))
+    names, q1, ang = np.array(names), np.array(q1), np.array(ang)
+    env = dict(os.environ, QSLC_EMU_MASK=rot, QSLC_EMU_MASK_H=had)
+    st = random_state(rng, n)
+    got = _run_pair1(tmp_path, "c128", st, names, q1, ang, dict(env, QSLC_SHFL="1"))
+    cpu = port.PortQubits(n, state=st)
+    for g, a, x in zip(names, q1, ang):
+        cpu.gate(str(g), int(a), None, float(x))
+    assert np.array_equal(bits(got), bits(cpu.state))
+    st64 = random_state(rng, n, np.complex64)
+    got64 = _run_pair1(tmp_path, "c64s", st64, names, q1, ang, dict(env, QSLC_SHFL="1"))
+    reg64 = _run_pair1(tmp_path, "c64r", st64, names, q1, ang, dict(env, QSLC_SHFL="0"))
+    assert np.array_equal(got64.view(np.uint32), reg64.view(np.uint32))
+    flat = np.full(1 << n, (1 + 1j) / np.sqrt(2.0 ** (n + 1)), dtype=np.complex128)
+    got = _run_pair1(tmp_path, "flat", flat, names, q1, ang, dict(env, QSLC_SHFL="1"))
+    cpu = port.PortQubits(n, state=flat)
+    for g, a, x in zip(names, q1, ang):
+        cpu.gate(str(g), int(a), None, float(x))
+    assert np.array_equal(bits(got), bits(cpu.state))

@@ -54,6 +54,9 @@ def test_batch_timing_picks_the_bench_instances():
     assert angles.size == int((2 * ns.astype(int) * ls.astype(int)).sum())
     with pytest.raises(SystemExit):
         batch_timing.main(["--first", "0", "--largest", "0"])
+    for bad in ("512,12", "512,x,2"):
+        with pytest.raises(SystemExit):
+            batch_timing.main(["--shape", bad])
 
 
 def np_sorted(a):
