@@ -9,7 +9,7 @@ CUDA-event time of each run.  The first run is the ncu capture target of
 one k_batch launch after a warm-up run (`-s 1 -c 1`):
 
     python batch_timing.py [--first 12] [--largest 4] [--dtype c128] [--repeat 3]
-                           [--shape THREADS,TILE_LOG2,CTAS_PER_SM]
+                           [--shape THREADS,TILE_LOG2,CTAS_PER_SM] [--max-qubits N]
 
 Without `--shape` the batch keeps its default launch shape (1024 threads,
 one CTA per SM, the larger tile); the benchmark's autotuner picks among
@@ -29,13 +29,19 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 
-def sub_batch(first: int, largest: int):
+def sub_batch(first: int, largest: int, max_qubits: int | None = None):
     """Indices of the chosen instances (ascending) and the sub-batch's
-    qubit counts, layer counts, angles and uniforms."""
+    qubit counts, layer counts, angles and uniforms.  With `max_qubits`,
+    the instances of more qubits among the first ones are left out (the
+    batch's arena, two buffers of the largest state per CTA, shrinks with
+    it)."""
     import bench
     from qsl_gb300 import batch_shards as bs
     _, ns, ls, _, angles, u = bench.batch_workload(types.SimpleNamespace(batch_instances=4096))
-    idx = np.unique(np.concatenate([np.arange(first), np.nonzero(ns == ns.max())[0][:largest]]))
+    head = np.arange(first)
+    if max_qubits is not None:
+        head = head[ns[head] <= max_qubits]
+    idx = np.unique(np.concatenate([head, np.nonzero(ns == ns.max())[0][:largest]]))
     return idx, bs.select(ns, ls, angles, u, bench.BATCH_SHOTS, idx)
 
 
@@ -46,6 +52,8 @@ def main(argv=None) -> None:
     ap.add_argument("--dtype", choices=["c128", "c64"], default="c128")
     ap.add_argument("--repeat", type=int, default=3)
     ap.add_argument("--shape", default=None, help="threads,tile_log2,ctas_per_sm")
+    ap.add_argument("--max-qubits", type=int, default=None,
+                    help="leave out the instances of more qubits among the first ones")
     a = ap.parse_args(argv)
     if a.first < 0 or a.largest < 0 or a.first + a.largest == 0 or a.first > 4096:
         ap.error("choose at least one instance, at most 4096 of the first ones")
@@ -61,7 +69,9 @@ def main(argv=None) -> None:
 
     import bench
     import qsl_gb300 as q
-    idx, (sn, sl, sa, su) = sub_batch(a.first, a.largest)
+    idx, (sn, sl, sa, su) = sub_batch(a.first, a.largest, a.max_qubits)
+    if idx.size == 0:
+        ap.error("no instance is left")
     b = q.Batch(sn, sl, bench.BATCH_SHOTS, dtype=np.complex128 if a.dtype == "c128" else np.complex64)
     if shape is not None:
         b.set_shape(*shape)
