@@ -54,6 +54,8 @@ def test_batch_timing_picks_the_bench_instances():
     assert angles.size == int((2 * ns.astype(int) * ls.astype(int)).sum())
     with pytest.raises(SystemExit):
         batch_timing.main(["--first", "0", "--largest", "0"])
+    idx, (ns, _, _, _) = batch_timing.sub_batch(300, 0, 14)
+    assert idx.size > 0 and int(ns.max()) <= 14 and np_sorted(idx)
     for bad in ("512,12", "512,x,2"):
         with pytest.raises(SystemExit):
             batch_timing.main(["--shape", bad])
