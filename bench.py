@@ -312,7 +312,9 @@ def batch_roofline(ns, ls, tile_log2, amp_bytes, kernel_ms, fp64):
     """Roofline of one batch launch.  HBM: an instance above a shared-memory
     tile writes its |0..0> state, reads and writes it twice per layer (two
     passes) and reads it once for the measurements, (2 + 4 L) x 2^n x amp
-    bytes; smaller instances never leave shared memory.  Arithmetic: the
+    bytes; smaller instances never leave shared memory; every instance's
+    2^n |a|^2 terms are written and read back once as doubles for the
+    sampling CDF, 16 x 2^n bytes.  Arithmetic: the
     FP64 operations the reference's loops perform (12 n 2^n per layer for
     rotateY and rotateZ on every qubit, 4 n 2^n for the probabilities, 4 x
     2^n for the CDF), against the FP64 pipe's rate -- the kernel puts part of
@@ -320,7 +322,7 @@ def batch_roofline(ns, ls, tile_log2, amp_bytes, kernel_ms, fp64):
     n = np.asarray(ns, dtype=np.int64)
     L = np.asarray(ls, dtype=np.int64)
     big = n > tile_log2
-    hbm_bytes = float(np.sum(np.where(big, (2 + 4 * L) << n, 0)) * amp_bytes)
+    hbm_bytes = float(np.sum(np.where(big, (2 + 4 * L) << n, 0)) * amp_bytes + np.sum(16 << n))
     # shared memory: a resident state is read and written by each rotateY
     # sweep, by the fused rotateZ sweep and by the ladder, per layer
     smem_bytes = float(np.sum(np.where(big, 0, (L * (n + 2)) << n)) * 2 * amp_bytes)

@@ -259,8 +259,12 @@ QSLC_API uint64_t qslc_fused_blocks(const qslc_state *s);
  * nlayers[i] layers of: rotateY on every qubit, rotateZ on every qubit,
  * controlNot(q, q+1) for q = 0..n-2; then prob(q, 0) and prob(q, 1) for
  * every q and `nshots` sampleAll draws.  All instances run in one
- * persistent kernel captured once in a CUDA graph.  Results are the bits
- * qsl's Default backend gives for the same calls. */
+ * persistent kernel, followed by one kernel that walks the sampling CDFs,
+ * both captured once in a CUDA graph.  Results are the bits qsl's Default
+ * backend gives for the same calls.  Device memory: the instances' inputs
+ * and results, 8 bytes per amplitude of every instance (the |a|^2 terms
+ * of the CDFs), and two state buffers per CTA of the largest instance
+ * when it does not fit a shared-memory tile. */
 typedef struct qslc_batch qslc_batch;
 QSLC_API int qslc_batch_create(int dtype, uint32_t ninst, const uint32_t *nqubits,
                                const uint32_t *nlayers, uint32_t nshots, qslc_batch **out);

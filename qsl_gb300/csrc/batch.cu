@@ -13,6 +13,12 @@
 // running sum reaches a uniform is its outcome, as drawSample's search
 // returns, measure.cpp:164-188).
 //
+// The CDF is one running sum per instance, a chain of dependent FP64 adds,
+// and the FP64 pipe takes as long for one active lane as for 32.  So
+// k_batch leaves each instance's |a|^2 terms in global memory and a second
+// kernel in the same graph, k_batch_cdf, walks the CDFs one instance per
+// thread: each FP64 instruction then advances up to 32 of them.
+//
 // Schedule: persistent CTAs pull instances, largest first, from an atomic
 // counter.  A state of at most one tile (2^k amplitudes of shared memory)
 // lives in shared memory for its whole circuit.  A larger state lives in
@@ -42,13 +48,14 @@ namespace qslc {
 namespace {
 
 constexpr int MAX_Q = 26;
+constexpr int CDF_THREADS = 128;   // 4 warps, 4 instances
 // How the rotation outputs are computed (complex128), as mode masks
 // (gatemath.cuh, OutMode): rotateY cycles over a thread's successive pairs
 // through three 8-bit masks, rotateZ over the qubits through three (2 bits
 // per output).  The build can set others (-DQSLC_BATCH_MODES_RY=...,
 // -DQSLC_BATCH_MODES_RZ=...) for tuning.
 #ifndef QSLC_BATCH_MODES_RY
-#define QSLC_BATCH_MODES_RY 0x151515u
+#define QSLC_BATCH_MODES_RY 0x555555u
 #endif
 #ifndef QSLC_BATCH_MODES_RZ
 #define QSLC_BATCH_MODES_RZ 0x050505u
@@ -61,6 +68,7 @@ struct InstDesc {
     uint64_t coef;      // offset of its coefficients: L*n*4 values (cy, sy, cz, sz)
     uint64_t probs;     // offset of its 2n probabilities
     uint64_t shots;     // offset of its shots (sorted-uniform order)
+    uint64_t norms;     // offset of its 2^n |a|^2 terms (doubles) for the sampling CDF
 };
 
 struct BatchArgs {
@@ -73,6 +81,8 @@ struct BatchArgs {
     const double *usorted;
     uint64_t *shots;
     uint32_t nshots;
+    double *norms;              // every instance's |a|^2 terms, in index order
+    const uint32_t *cdf_order;  // instances by qubit count, largest first
     void *arena;
     uint64_t slot_amps;     // amplitudes per arena buffer (two buffers per slot)
     unsigned tile_log2;     // k: the shared-memory tile holds 2^k amplitudes
@@ -211,89 +221,84 @@ __device__ __forceinline__ cplx<T> rz_all(cplx<T> a, uint64_t x, uint32_t n, con
     return a;
 }
 
-// The measurements of one instance from its final state `st` (shared or
-// global memory, natural order).
+// The sampling CDF's test u <= run, for u in [0, 1) and run >= 0: the bit
+// patterns of non-negative doubles order like their values, so integer
+// compares keep it off the FP64 pipe.
+__device__ __forceinline__ bool cdf_reached(double u, double run)
+{
+    return __double_as_longlong(u) <= __double_as_longlong(run);
+}
+
+// The measurements of one instance from its final state `st` in shared
+// memory (natural order): its 2n probabilities, and its |a|^2 terms for the
+// sampling CDF written to `gn` (as doubles).  `nrm`, when not null, is room
+// for 2^n values of T: every thread then computes the terms once, in
+// parallel, and the probability sums read them instead of recomputing them.
 template <class T>
-__device__ void finish_instance(const cplx<T> *st, const InstDesc &d, T *__restrict__ probs,
-                                const double *__restrict__ u, uint64_t *__restrict__ shots,
-                                uint32_t nshots)
+__device__ void finish_instance(const cplx<T> *st, T *nrm, const InstDesc &d, T *__restrict__ probs,
+                                double *__restrict__ gn)
 {
     const uint32_t n = d.n;
     const uint64_t dim = uint64_t(1) << n, half = dim >> 1;
     const unsigned tid = threadIdx.x;
+    __syncthreads();                                  // the state's last writes
+    for (uint64_t i = tid; i < dim; i += blockDim.x) {
+        const T t = norm2_rn(st[i].x, st[i].y);
+        if (nrm) nrm[i] = t;
+        gn[i] = double(t);
+    }
+    if (nrm) __syncthreads();
+    auto term = [&](uint64_t i) {
+        if (nrm) return nrm[i];
+        const cplx<T> a = st[i];
+        return norm2_rn(a.x, a.y);
+    };
     // prob(q, o): sequential Fp sums in index order (measure.cpp:126-147)
     if (tid < 2 * n) {
         const uint32_t q = tid >> 1, o = tid & 1;
         const uint64_t ob = uint64_t(o) << q;
         T p = T(0);
-        for (uint64_t j = 0; j < half; j++) {
-            const cplx<T> a = st[insert0(j, q) | ob];
-            p = rn<T>::add(p, norm2_rn(a.x, a.y));
-        }
+        for (uint64_t j = 0; j < half; j++) p = rn<T>::add(p, term(insert0(j, q) | ob));
         probs[d.probs + 2 * q + o] = p;
-    } else if (tid == 2 * n) {
-        // sampling: the double running sum over all amplitudes, merged
-        // against the sorted uniforms (measure.cpp:60-78, :164-188)
-        uint64_t *out = shots + d.shots;
-        uint32_t k = 0;
-        double run = 0.0;
-        for (uint64_t i = 0; i < dim && k < nshots; i++) {
-            const cplx<T> a = st[i];
-            run = __dadd_rn(run, double(norm2_rn(a.x, a.y)));
-            while (k < nshots && u[k] <= run) out[k++] = i;
-        }
-        for (; k < nshots; k++) out[k] = 0;           // above the total: index 0
     }
     __syncthreads();
 }
 
-// The measurements of a large instance: the final state passes through
-// shared memory one tile at a time, and every sum walks its terms of the
-// tile in index order, so each keeps the reference's sequential order while
-// reading shared instead of global memory.
+// The measurements of a large instance: the final state passes one tile at
+// a time; all threads turn a tile into its |a|^2 terms, in shared memory for
+// the probability sums and in `gn` for the sampling CDF, and every sum walks
+// its terms of the tile in index order, so each keeps the reference's
+// sequential order while reading each term once from global memory.
 template <class T>
 __device__ void finish_big(const cplx<T> *st, cplx<T> *sm, unsigned k, const InstDesc &d,
-                           T *__restrict__ probs, const double *__restrict__ u,
-                           uint64_t *__restrict__ shots, uint32_t nshots)
+                           T *__restrict__ probs, double *__restrict__ gn)
 {
     const uint32_t n = d.n;
     const uint64_t dim = uint64_t(1) << n, chunk = uint64_t(1) << k;
     const unsigned tid = threadIdx.x, nt = blockDim.x;
     const uint32_t q = tid >> 1, o = tid & 1;
+    T *nrm = reinterpret_cast<T *>(sm);
     T p = T(0);
-    double run = 0.0;
-    uint32_t kk = 0;
-    uint64_t *out = shots + d.shots;
     for (uint64_t c = 0; c < (dim >> k); c++) {
         __syncthreads();
-        for (uint64_t i = tid; i < chunk; i += nt) sm[i] = st[(c << k) + i];
+        for (uint64_t i = tid; i < chunk; i += nt) {
+            const cplx<T> a = st[(c << k) + i];
+            const T t = norm2_rn(a.x, a.y);
+            nrm[i] = t;
+            gn[(c << k) + i] = double(t);
+        }
         __syncthreads();
         if (tid < 2 * n) {
             // prob(q, o): the terms with bit q == o (measure.cpp:126-147)
             if (q < k) {
                 const uint64_t ob = uint64_t(o) << q;
-                for (uint64_t j = 0; j < (chunk >> 1); j++) {
-                    const cplx<T> a = sm[insert0(j, q) | ob];
-                    p = rn<T>::add(p, norm2_rn(a.x, a.y));
-                }
+                for (uint64_t j = 0; j < (chunk >> 1); j++) p = rn<T>::add(p, nrm[insert0(j, q) | ob]);
             } else if (((c >> (q - k)) & 1) == o) {
-                for (uint64_t i = 0; i < chunk; i++) {
-                    const cplx<T> a = sm[i];
-                    p = rn<T>::add(p, norm2_rn(a.x, a.y));
-                }
-            }
-        } else if (tid == 2 * n) {
-            // the sampling CDF merged against the sorted uniforms
-            for (uint64_t i = 0; i < chunk && kk < nshots; i++) {
-                const cplx<T> a = sm[i];
-                run = __dadd_rn(run, double(norm2_rn(a.x, a.y)));
-                while (kk < nshots && u[kk] <= run) out[kk++] = (c << k) + i;
+                for (uint64_t i = 0; i < chunk; i++) p = rn<T>::add(p, nrm[i]);
             }
         }
     }
     if (tid < 2 * n) probs[d.probs + 2 * q + o] = p;
-    else if (tid == 2 * n)
-        for (; kk < nshots; kk++) out[kk] = 0;       // above the total: index 0
     __syncthreads();
 }
 
@@ -402,15 +407,137 @@ __global__ void __launch_bounds__(1024) k_batch(BatchArgs a)
         if (w >= a.ninst) break;
         const uint32_t id = a.order[w];
         const InstDesc d = a.inst[id];
-        const double *u = a.usorted + uint64_t(id) * a.nshots;
         if (d.n <= a.tile_log2) {
             run_small<T>(sm, lc, d, coef);
-            finish_instance<T>(sm, d, probs, u, a.shots, a.nshots);
+            // the terms go after the state when it fills at most half the tile
+            T *nrm = d.n < a.tile_log2 ? reinterpret_cast<T *>(sm + (uint64_t(1) << d.n)) : nullptr;
+            finish_instance<T>(sm, nrm, d, probs, a.norms + d.norms);
         } else {
             const cplx<T> *fin = run_big<T>(sm, lc, d, coef, slot, slot + a.slot_amps, a.tile_log2);
-            finish_big<T>(fin, sm, a.tile_log2, d, probs, u, a.shots, a.nshots);
+            finish_big<T>(fin, sm, a.tile_log2, d, probs, a.norms + d.norms);
         }
     }
+}
+
+// The sampling CDFs, after k_batch, one instance per warp (instance
+// cdf_order[w] for warp w).  A uniform's outcome is the first index whose
+// running double sum of |a|^2 terms reaches it, index 0 when none does
+// (measure.cpp:60-78, :164-188).  The running sum s is exact at all times:
+//   - while s is normal, in binade e, a round of 32 x CDF_RUN terms runs in
+//     parallel: each lane takes CDF_RUN consecutive terms, a warp scan of
+//     their grid-step transducers (replay.cuh) gives every lane the grid
+//     position where its run starts, and each lane walks its run; the round
+//     stops before the first term whose sum would leave the binade (or that
+//     is too big for it), which is then added on its own with one FP64 add;
+//   - while s is zero, runs of zero terms are skipped 32 at a time, and
+//     while it is subnormal, terms are added one at a time.
+// After every term, all uniforms the sum has reached take that term's index,
+// so the outcomes are the sequential merge's.
+constexpr unsigned CDF_RUN = 16;
+constexpr uint64_t CDF_NONE = ~uint64_t(0);
+
+__device__ __forceinline__ Tx shfl_up_tx(const Tx &t, unsigned off)
+{
+    Tx r;
+    r.d[0] = __shfl_up_sync(0xFFFFFFFFu, (unsigned long long)t.d[0], off);
+    r.d[1] = __shfl_up_sync(0xFFFFFFFFu, (unsigned long long)t.d[1], off);
+    return r;
+}
+
+__global__ void __launch_bounds__(CDF_THREADS) k_batch_cdf(BatchArgs a)
+{
+    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned lane = threadIdx.x & 31;
+    if (w >= a.ninst) return;                             // whole warps
+    const uint32_t id = a.cdf_order[w];
+    const InstDesc d = a.inst[id];
+    const double *__restrict__ nr = a.norms + d.norms;
+    const double *__restrict__ u = a.usorted + uint64_t(id) * a.nshots;
+    uint64_t *__restrict__ out = a.shots + d.shots;
+    const uint64_t dim = uint64_t(1) << d.n;
+    const uint32_t ns = a.nshots;
+    uint32_t k = 0;                                       // next uniform
+    double s = 0.0;                                       // the sum of terms 0..i-1
+    uint64_t i = 0;                                       // next term
+    // every uniform the sum s has reached takes index `idx`
+    auto consume = [&](uint64_t idx) {
+        while (k < ns && cdf_reached(u[k], s)) {
+            if (lane == 0) out[k] = idx;
+            k++;
+        }
+    };
+    while (i < dim && k < ns) {
+        const int e = binade(s);
+        if (e < fp_traits<double>::EMIN) {
+            if (__double_as_longlong(s) == 0) {
+                // zero so far: skip to the first nonzero term of the next 32
+                const uint64_t j = i + lane;
+                const unsigned nz = __ballot_sync(0xFFFFFFFFu, j < dim && __double_as_longlong(nr[j]) != 0);
+                consume(i);                               // u == 0 is reached at term i
+                if (!nz) {
+                    i = i + 32 < dim ? i + 32 : dim;
+                    continue;
+                }
+                i += unsigned(__ffs(nz) - 1);
+            }
+            s = __dadd_rn(s, nr[i]);                      // subnormal (or zero) sum: one term
+            consume(i);
+            i++;
+            continue;
+        }
+        // a round of terms [i, end) in binade e
+        const uint64_t m0 = (uint64_t(__double_as_longlong(s)) & ((uint64_t(1) << 52) - 1)) | (uint64_t(1) << 52);
+        const uint64_t end = i + 32 * CDF_RUN < dim ? i + 32 * CDF_RUN : dim;
+        const uint64_t base = i + uint64_t(lane) * CDF_RUN;
+        const unsigned len = base < end ? unsigned(end - base < CDF_RUN ? end - base : CDF_RUN) : 0u;
+        bool big = false;
+        const Tx mine = run_effect<double>(nr + base, len, e, big);
+        Tx incl = mine;
+        for (unsigned off = 1; off < 32; off <<= 1) {
+            const Tx o = shfl_up_tx(incl, off);
+            if (lane >= off) incl = tx_then(o, incl);
+        }
+        Tx excl = shfl_up_tx(incl, 1);
+        if (lane == 0) excl = tx_identity();
+        const uint64_t pos0 = m0 + excl.d[m0 & 1];        // grid position before this lane's run
+        uint64_t pos = pos0;
+        const unsigned walked = run_walk<double>(nr + base, len, e, pos);
+        uint64_t bad = walked < len ? base + walked : CDF_NONE;
+        for (unsigned off = 16; off; off >>= 1) {
+            const uint64_t o = __shfl_xor_sync(0xFFFFFFFFu, (unsigned long long)bad, off);
+            bad = o < bad ? o : bad;
+        }
+        const uint64_t stop = bad == CDF_NONE ? end : bad;
+        // the position after term stop - 1: where the lane holding `stop`
+        // stopped, or where the lane holding the round's last term ended
+        const uint64_t last = bad == CDF_NONE ? end - 1 : stop;
+        const unsigned holder = unsigned((last - i) / CDF_RUN);
+        const uint64_t pend = __shfl_sync(0xFFFFFFFFu, (unsigned long long)pos, holder);
+        // uniforms reached inside [i, stop): the first term whose position
+        // reaches the uniform's grid target
+        const bool live = len && base < stop;
+        while (k < ns) {
+            const uint64_t tgt = grid_ceil<double>(u[k], e);
+            if (tgt > pend) break;
+            const unsigned hit = __ballot_sync(0xFFFFFFFFu, live && pos >= tgt);
+            if (!hit) break;                              // not reached: pend >= tgt rules it out
+            const unsigned L = unsigned(__ffs(hit) - 1);
+            uint64_t j = 0;
+            if (lane == L) j = base + run_find<double>(nr + base, len, e, pos0, tgt);
+            j = __shfl_sync(0xFFFFFFFFu, (unsigned long long)j, L);
+            if (lane == 0) out[k] = j;
+            k++;
+        }
+        s = __longlong_as_double((long long)((uint64_t(e + 1023) << 52) | (pend - (uint64_t(1) << 52))));
+        i = stop;
+        if (bad != CDF_NONE) {
+            s = __dadd_rn(s, nr[i]);                      // the term that leaves the binade
+            consume(i);
+            i++;
+        }
+    }
+    for (; k < ns; k++)
+        if (lane == 0) out[k] = 0;                        // above the total: index 0
 }
 
 }  // namespace
@@ -429,11 +556,12 @@ struct qslc_batch {
     int dtype = QSLC_C128;
     uint32_t ninst = 0, nshots = 0, nmax = 0;
     std::vector<InstDesc> inst;
-    std::vector<uint32_t> order;
-    uint64_t ncoef = 0, nprobs = 0, nshot_total = 0;
+    std::vector<uint32_t> order, cdf_order;
+    uint64_t ncoef = 0, nprobs = 0, nshot_total = 0, nnorm_total = 0;
     cudaStream_t stream = nullptr;
     void *d_inst = nullptr, *d_order = nullptr, *d_counter = nullptr, *d_coef = nullptr;
     void *d_probs = nullptr, *d_u = nullptr, *d_shots = nullptr, *d_arena = nullptr;
+    void *d_norms = nullptr, *d_cdf_order = nullptr;
     uint64_t arena_bytes = 0, slot_amps = 0;
     BatchShape shape;
     unsigned grid = 0;
@@ -464,7 +592,7 @@ void batch_free(qslc_batch *b)
     if (b->stream) cudaStreamSynchronize(b->stream);
     drop_graph(b);
     for (void *p : {b->d_inst, b->d_order, b->d_counter, b->d_coef, b->d_probs, b->d_u, b->d_shots,
-                    b->d_arena})
+                    b->d_arena, b->d_norms, b->d_cdf_order})
         if (p) cudaFree(p);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -517,12 +645,15 @@ int capture(qslc_batch *b, const BatchShape &s)
     a.usorted = static_cast<const double *>(b->d_u);
     a.shots = static_cast<uint64_t *>(b->d_shots);
     a.nshots = b->nshots;
+    a.norms = static_cast<double *>(b->d_norms);
+    a.cdf_order = static_cast<const uint32_t *>(b->d_cdf_order);
     a.arena = b->d_arena;
     a.slot_amps = b->slot_amps;
     a.tile_log2 = s.tile_log2;
     QSLC_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned), b->stream);
     k_batch<T><<<grid, s.threads, smem, b->stream>>>(a);
+    k_batch_cdf<<<(b->ninst + CDF_THREADS / 32 - 1) / (CDF_THREADS / 32), CDF_THREADS, 0, b->stream>>>(a);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
@@ -644,7 +775,9 @@ extern "C" int qslc_batch_create(int dtype, uint32_t ninst, const uint32_t *nqub
         d.coef = b->ncoef;
         d.probs = b->nprobs;
         d.shots = b->nshot_total;
+        d.norms = b->nnorm_total;
         b->ncoef += uint64_t(d.L) * d.n * 4;
+        b->nnorm_total += uint64_t(1) << d.n;
         b->nprobs += 2 * uint64_t(d.n);
         b->nshot_total += nshots;
         b->nmax = std::max(b->nmax, d.n);
@@ -655,6 +788,12 @@ extern "C" int qslc_batch_create(int dtype, uint32_t ninst, const uint32_t *nqub
     std::stable_sort(b->order.begin(), b->order.end(), [&](uint32_t x, uint32_t y) {
         return (uint64_t(b->inst[x].L) << b->inst[x].n) > (uint64_t(b->inst[y].L) << b->inst[y].n);
     });
+    // the CDF walks: one instance per thread, a warp's instances of about
+    // the same length
+    b->cdf_order.resize(ninst);
+    std::iota(b->cdf_order.begin(), b->cdf_order.end(), 0u);
+    std::stable_sort(b->cdf_order.begin(), b->cdf_order.end(),
+                     [&](uint32_t x, uint32_t y) { return b->inst[x].n > b->inst[y].n; });
     const size_t fb = dtype == QSLC_C128 ? 8 : 4;
     int rc = QSLC_OK;
     auto alloc = [&](void **p, size_t bytes) {
@@ -671,11 +810,15 @@ extern "C" int qslc_batch_create(int dtype, uint32_t ninst, const uint32_t *nqub
     alloc(&b->d_probs, b->nprobs * fb);
     alloc(&b->d_u, b->nshot_total * 8);
     alloc(&b->d_shots, b->nshot_total * 8);
+    alloc(&b->d_norms, b->nnorm_total * 8);
+    alloc(&b->d_cdf_order, ninst * 4);
     if (!rc && cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess)
         rc = fail(QSLC_ECUDA, "stream creation failed");
     if (!rc && cudaMemcpy(b->d_inst, b->inst.data(), ninst * sizeof(InstDesc), cudaMemcpyHostToDevice) != cudaSuccess)
         rc = fail(QSLC_ECUDA, "upload failed");
     if (!rc && cudaMemcpy(b->d_order, b->order.data(), ninst * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+        rc = fail(QSLC_ECUDA, "upload failed");
+    if (!rc && cudaMemcpy(b->d_cdf_order, b->cdf_order.data(), ninst * 4, cudaMemcpyHostToDevice) != cudaSuccess)
         rc = fail(QSLC_ECUDA, "upload failed");
     if (!rc) {
         const auto c = candidates(b);

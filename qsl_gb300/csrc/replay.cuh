@@ -142,6 +142,83 @@ QSLC_HD Tx tx_then(const Tx &a, const Tx &b)
     return r;
 }
 
+// ceil(u / u_e) with u_e = 2^(e - MANT): the first grid position of binade
+// e at or above u >= 0, saturating at TX_SAT.  A sum at grid position N of
+// binade e has reached u exactly when grid_ceil(u, e) <= N.
+template <class A>
+QSLC_HD uint64_t grid_ceil(A u, int e)
+{
+    using T = fp_traits<A>;
+    auto b = to_bits(u);
+    int ef = int((b >> T::MANT) & T::EXPMASK);
+    uint64_t m = uint64_t(b & ((typename T::bits_t(1) << T::MANT) - 1));
+    if (ef == 0 && m == 0) return 0;
+    int lsb;
+    if (ef != 0) {
+        m |= uint64_t(1) << T::MANT;
+        lsb = ef - T::BIAS - T::MANT;
+    } else {
+        lsb = T::EMIN - T::MANT;
+    }
+    const int sh = (e - T::MANT) - lsb;       // u / u_e = m * 2^-sh
+    if (sh <= 0) {
+        const int ls = -sh;
+        if (ls >= 62 - T::MANT) return TX_SAT; // m < 2^(MANT+1): m << ls < 2^62 below this
+        return m << ls;
+    }
+    if (sh >= 64) return 1;                    // 0 < u / u_e < 1
+    const uint64_t q = m >> sh;
+    return q + ((m & ((uint64_t(1) << sh) - 1)) != 0 ? 1 : 0);
+}
+
+// Runs of consecutive terms of a running sum in binade e, for walking a
+// sampling CDF a warp at a time: each lane takes one run, run_effect gives
+// the run's Tx (composed across lanes by a scan), run_walk advances a grid
+// position through the run from where the lanes before left it, and
+// run_find locates the term at which the position reaches a uniform's
+// target.  The position must stay below 2^(MANT+1) (the binade's end);
+// run_walk stops before the first term that would take it there, or whose
+// step count does not fit the binade.
+template <class A>
+QSLC_HD Tx run_effect(const A *p, unsigned len, int e, bool &big_any)
+{
+    Tx t = tx_identity();
+    for (unsigned r = 0; r < len; r++) {
+        bool tie, big;
+        const uint64_t q = grid_steps<A>(p[r], e, tie, big);
+        big_any |= big;
+        t = tx_then(t, tx_term(q, tie));
+    }
+    return t;
+}
+
+template <class A>
+QSLC_HD unsigned run_walk(const A *p, unsigned len, int e, uint64_t &pos)
+{
+    const uint64_t lim = uint64_t(1) << (fp_traits<A>::MANT + 1);
+    for (unsigned r = 0; r < len; r++) {
+        bool tie, big;
+        const uint64_t q = grid_steps<A>(p[r], e, tie, big);
+        if (big || pos >= lim) return r;
+        const uint64_t step = tx_term(q, tie).d[pos & 1];
+        if (step >= lim - pos) return r;
+        pos += step;
+    }
+    return len;
+}
+
+template <class A>
+QSLC_HD unsigned run_find(const A *p, unsigned len, int e, uint64_t pos, uint64_t target)
+{
+    for (unsigned r = 0; r < len; r++) {
+        bool tie, big;
+        const uint64_t q = grid_steps<A>(p[r], e, tie, big);
+        pos += tx_term(q, tie).d[pos & 1];
+        if (pos >= target) return r;
+    }
+    return len;
+}
+
 // |a|^2 as the reference computes it: RN(RN(re*re) + RN(im*im))
 // (measure.cpp:69-70, :141-142).
 QSLC_HD double norm2_rn(double re, double im)

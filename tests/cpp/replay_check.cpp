@@ -6,8 +6,10 @@
 // associative (any grouping gives the same counts).
 #include "replay.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <random>
 #include <vector>
 
@@ -68,9 +70,193 @@ static int check(int trials)
     return fails;
 }
 
+// grid_ceil(u, e) is the first grid position of binade e at or above u.
+static int check_ceil(int trials)
+{
+    int fails = 0;
+    for (int t = 0; t < trials; t++) {
+        const int e = -int(rng() % 60);
+        double u = std::ldexp(double(rng() >> 11) * 0x1p-53, -int(rng() % 70));
+        if (rng() % 8 == 0) u = std::ldexp(double(rng() % 1000), e - 52);   // on the grid
+        if (rng() % 16 == 0) u = 0;
+        const uint64_t n = grid_ceil<double>(u, e);
+        if (n >= (uint64_t(1) << 53)) continue;
+        const bool ok = (n == 0 && u == 0) ||
+                        (n > 0 && std::ldexp(double(n - 1), e - 52) < u && u <= std::ldexp(double(n), e - 52));
+        if (!ok && fails++ < 5) std::printf("grid_ceil(%a, %d) = %llu\n", u, e, (unsigned long long)n);
+    }
+    std::printf("grid_ceil: %d fails\n", fails);
+    return fails;
+}
+
+static uint64_t bits_of(double x)
+{
+    uint64_t b;
+    std::memcpy(&b, &x, 8);
+    return b;
+}
+
+// The reference's merge: the sequential running sum against sorted uniforms.
+static std::vector<uint64_t> cdf_sequential(const std::vector<double> &p, const std::vector<double> &u)
+{
+    std::vector<uint64_t> out(u.size(), 0);
+    size_t k = 0;
+    double run = 0;
+    for (size_t i = 0; i < p.size() && k < u.size(); i++) {
+        volatile double nx = run + p[i];
+        run = nx;
+        while (k < u.size() && u[k] <= run) out[k++] = i;
+    }
+    return out;
+}
+
+// The batching form's CDF walk (k_batch_cdf in batch.cu), its 32 lanes
+// emulated one after another: rounds of 32 runs of `run` terms in one
+// binade, a scan of the runs' transducers, the walks, the first term that
+// leaves the binade added on its own; zero sums skip zero terms 32 at a
+// time, subnormal sums add one term at a time.
+static std::vector<uint64_t> cdf_rounds(const std::vector<double> &p, const std::vector<double> &u,
+                                        unsigned run)
+{
+    const uint64_t dim = p.size(), NONE = ~uint64_t(0);
+    const size_t ns = u.size();
+    std::vector<uint64_t> out(ns, 0);
+    size_t k = 0;
+    double s = 0;
+    uint64_t i = 0;
+    auto consume = [&](uint64_t idx) {
+        while (k < ns && bits_of(u[k]) <= bits_of(s)) out[k++] = idx;
+    };
+    while (i < dim && k < ns) {
+        const int e = binade<double>(s);
+        if (e < fp_traits<double>::EMIN) {
+            if (bits_of(s) == 0) {
+                unsigned first = 32;
+                for (unsigned l = 0; l < 32; l++)
+                    if (i + l < dim && bits_of(p[i + l]) != 0) {
+                        first = l;
+                        break;
+                    }
+                consume(i);
+                if (first == 32) {
+                    i = i + 32 < dim ? i + 32 : dim;
+                    continue;
+                }
+                i += first;
+            }
+            volatile double nx = s + p[i];
+            s = nx;
+            consume(i);
+            i++;
+            continue;
+        }
+        const uint64_t m0 = (bits_of(s) & ((uint64_t(1) << 52) - 1)) | (uint64_t(1) << 52);
+        const uint64_t end = i + 32 * run < dim ? i + 32 * run : dim;
+        uint64_t base[32], pos0[32], pos[32];
+        unsigned len[32];
+        Tx acc = tx_identity();
+        uint64_t bad = NONE;
+        for (unsigned l = 0; l < 32; l++) {
+            base[l] = i + uint64_t(l) * run;
+            len[l] = base[l] < end ? unsigned(end - base[l] < run ? end - base[l] : run) : 0u;
+            bool big = false;
+            const Tx t = run_effect<double>(p.data() + base[l], len[l], e, big);
+            pos0[l] = m0 + acc.d[m0 & 1];
+            acc = tx_then(acc, t);
+            pos[l] = pos0[l];
+            const unsigned walked = run_walk<double>(p.data() + base[l], len[l], e, pos[l]);
+            if (walked < len[l] && base[l] + walked < bad) bad = base[l] + walked;
+        }
+        const uint64_t stop = bad == NONE ? end : bad;
+        const uint64_t last = bad == NONE ? end - 1 : stop;
+        const uint64_t pend = pos[(last - i) / run];
+        while (k < ns) {
+            const uint64_t tgt = grid_ceil<double>(u[k], e);
+            if (tgt > pend) break;
+            unsigned L = 32;
+            for (unsigned l = 0; l < 32; l++)
+                if (len[l] && base[l] < stop && pos[l] >= tgt) {
+                    L = l;
+                    break;
+                }
+            if (L == 32) break;
+            out[k++] = base[L] + run_find<double>(p.data() + base[L], len[L], e, pos0[L], tgt);
+        }
+        const uint64_t sb = (uint64_t(e + 1023) << 52) | (pend - (uint64_t(1) << 52));
+        std::memcpy(&s, &sb, 8);
+        i = stop;
+        if (bad != NONE) {
+            volatile double nx = s + p[i];
+            s = nx;
+            consume(i);
+            i++;
+        }
+    }
+    return out;
+}
+
+// Term sequences that exercise every path of the walk: |a|^2 of random
+// states, leading zeros, equal dyadic terms (exact sums), terms from a few
+// dyadic values (ties), subnormal terms, and a term far above the sum.
+static int check_cdf_walk(int trials)
+{
+    int fails = 0, cases = 0;
+    for (int t = 0; t < trials; t++) {
+        const int n = 3 + int(rng() % 12);
+        const uint64_t dim = uint64_t(1) << n;
+        std::vector<double> p(dim);
+        const int kind = int(rng() % 7);
+        std::normal_distribution<double> g;
+        double norm = 0;
+        for (auto &x : p) {
+            const double re = g(rng), im = g(rng);
+            x = re * re + im * im;
+            norm += x;
+        }
+        for (auto &x : p) x /= norm;
+        if (kind == 1)
+            for (uint64_t j = 0; j < dim / 2 + rng() % (dim / 2); j++) p[j] = 0;
+        if (kind == 2)
+            for (auto &x : p) x = std::ldexp(1.0, -n);
+        if (kind == 3) {
+            const double vals[4] = {0x1p-20, 0x1.8p-30, 0x1.0000000000001p-12, 0x1p-55};
+            for (auto &x : p) x = vals[rng() % 4];
+        }
+        if (kind == 4)
+            for (uint64_t j = 0; j < dim; j++) p[j] = j < dim / 2 ? std::ldexp(double(rng() % 7), -1074) : p[j];
+        if (kind == 5) p[rng() % dim] = 0.75;
+        if (kind == 6)
+            for (auto &x : p) x = double(float(x));
+        std::vector<double> cdf(dim);
+        double run = 0;
+        for (uint64_t j = 0; j < dim; j++) {
+            volatile double nx = run + p[j];
+            run = nx;
+            cdf[j] = run;
+        }
+        std::vector<double> u;
+        for (int j = 0; j < 64; j++) u.push_back(double(rng() >> 11) * 0x1p-53);
+        for (int j = 0; j < 16; j++) u.push_back(cdf[rng() % dim]);                 // on a partial sum
+        for (int j = 0; j < 8; j++) u.push_back(std::nextafter(cdf[rng() % dim], 1.0));
+        u.push_back(0.0);
+        u.push_back(std::nextafter(run, 2.0));                                       // above the total
+        std::sort(u.begin(), u.end());
+        const auto want = cdf_sequential(p, u);
+        for (unsigned r : {1u, 3u, 16u}) {
+            cases++;
+            if (cdf_rounds(p, u, r) != want && fails++ < 5)
+                std::printf("cdf walk differs: kind %d, n %d, run %u\n", kind, n, r);
+        }
+    }
+    std::printf("cdf walk: %d cases, %d fails\n", cases, fails);
+    return fails;
+}
+
 int main()
 {
     int f = check<double, double>(3000) + check<double, float>(3000) + check<float, float>(3000);
+    f += check_ceil(200000);
+    f += check_cdf_walk(1500);
     if (f) return 1;
     std::puts("replay ok");
     return 0;

@@ -96,3 +96,52 @@ def test_every_launch_shape_matches_oracle(qsl, port, dtype):
     assert ms > 0 and tuple(b.shape()[x] for x in ("threads", "tile_log2", "ctas_per_sm")) in shapes
     probs, shots = b.run(angles, u)
     assert all(np.array_equal(probs[i], want[i][0]) for i in range(ns.size))
+
+
+@pytest.mark.parametrize("dtype", [np.complex128, np.complex64])
+def test_batch_sampling_on_exact_and_tied_sums(qsl, port, dtype):
+    """The sampling CDFs walk in rounds within one binade, adding the term
+    that leaves it on its own (k_batch_cdf).  Angles drawn from multiples of
+    pi/4 make states with many equal and exactly zero |a|^2 terms -- exact
+    partial sums, ties, leading zeros -- and uniforms sit on the
+    reference's own partial sums and just above them; every shot must be
+    the oracle's."""
+    rng = np.random.default_rng(31)
+    fp32 = dtype == np.complex64
+    ns = np.array([3, 6, 9, 12, 14, 15], dtype=np.uint32)
+    ls = np.array([1, 2, 1, 2, 1, 2], dtype=np.uint32)
+    nshots = 200
+    b = qsl.Batch(ns, ls, nshots, dtype=dtype)
+    angles = rng.choice(np.array([0.0, 0.5, 1.0, 1.5, 0.25]) * np.pi, b.angle_count)
+    if fp32:
+        angles = angles.astype(np.float32).astype(np.float64)
+    us, at = [], 0
+    want = []
+    for i, (n, L) in enumerate(zip(ns, ls)):
+        n, L = int(n), int(L)
+        cnt = 2 * n * L
+        sim = port.PortQubits(n, fp32=fp32)
+        a = angles[at:at + cnt].reshape(L, n, 2)
+        at += cnt
+        for l in range(L):
+            for q in range(n):
+                sim.gate("rotateY", q, None, a[l, q, 0])
+            for q in range(n):
+                sim.gate("rotateZ", q, None, a[l, q, 1])
+            for q in range(n - 1):
+                sim.gate("controlNot", q, q + 1)
+        st = sim.state
+        re, im = st.real, st.imag
+        p = (re * re + im * im).astype(np.float64)       # RN(RN(re^2) + RN(im^2)) in the state's type
+        cdf = np.cumsum(p)                                # sequential, in index order
+        pick = cdf[rng.integers(0, cdf.size, nshots // 2)]
+        u = np.concatenate([pick, np.nextafter(pick, 1.0)[: nshots // 4],
+                            rng.random(nshots - nshots // 2 - nshots // 4)])
+        u = np.clip(u, 0.0, np.nextafter(1.0, 0.0))
+        if fp32:
+            u = u.astype(np.float32).astype(np.float64)
+        us.append(u)
+        want.append(sim.sample_all(u))
+    probs, shots = b.run(angles, np.concatenate(us))
+    for i in range(ns.size):
+        assert np.array_equal(shots[i], want[i]), (i, int(ns[i]))
