@@ -486,12 +486,13 @@ __global__ void __launch_bounds__(CDF_THREADS) k_batch_cdf(BatchArgs a)
             continue;
         }
         // a round of terms [i, end) in binade e
-        const uint64_t m0 = (uint64_t(__double_as_longlong(s)) & ((uint64_t(1) << 52) - 1)) | (uint64_t(1) << 52);
+        const uint64_t m0 = grid_pos(s);
         const uint64_t end = i + 32 * CDF_RUN < dim ? i + 32 * CDF_RUN : dim;
         const uint64_t base = i + uint64_t(lane) * CDF_RUN;
         const unsigned len = base < end ? unsigned(end - base < CDF_RUN ? end - base : CDF_RUN) : 0u;
+        auto run = [nr, base](unsigned r) { return nr[base + r]; };
         bool big = false;
-        const Tx mine = run_effect<double>(nr + base, len, e, big);
+        const Tx mine = run_effect<double>(run, len, e, big);
         Tx incl = mine;
         for (unsigned off = 1; off < 32; off <<= 1) {
             const Tx o = shfl_up_tx(incl, off);
@@ -501,7 +502,7 @@ __global__ void __launch_bounds__(CDF_THREADS) k_batch_cdf(BatchArgs a)
         if (lane == 0) excl = tx_identity();
         const uint64_t pos0 = m0 + excl.d[m0 & 1];        // grid position before this lane's run
         uint64_t pos = pos0;
-        const unsigned walked = run_walk<double>(nr + base, len, e, pos);
+        const unsigned walked = run_walk<double>(run, len, e, pos);
         uint64_t bad = walked < len ? base + walked : CDF_NONE;
         for (unsigned off = 16; off; off >>= 1) {
             const uint64_t o = __shfl_xor_sync(0xFFFFFFFFu, (unsigned long long)bad, off);
@@ -523,12 +524,12 @@ __global__ void __launch_bounds__(CDF_THREADS) k_batch_cdf(BatchArgs a)
             if (!hit) break;                              // not reached: pend >= tgt rules it out
             const unsigned L = unsigned(__ffs(hit) - 1);
             uint64_t j = 0;
-            if (lane == L) j = base + run_find<double>(nr + base, len, e, pos0, tgt);
+            if (lane == L) j = base + run_find<double>(run, len, e, pos0, tgt);
             j = __shfl_sync(0xFFFFFFFFu, (unsigned long long)j, L);
             if (lane == 0) out[k] = j;
             k++;
         }
-        s = __longlong_as_double((long long)((uint64_t(e + 1023) << 52) | (pend - (uint64_t(1) << 52))));
+        s = grid_at<double>(pend, e);
         i = stop;
         if (bad != CDF_NONE) {
             s = __dadd_rn(s, nr[i]);                      // the term that leaves the binade

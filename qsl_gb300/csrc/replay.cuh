@@ -74,26 +74,29 @@ QSLC_HD int binade(A x)
 }
 
 // Integer number of grid steps of binade e that adding p >= 0 moves a sum
-// lying in binade e: rne(p / u_e) with u_e = 2^(e - MANT).  `tie` is set
-// when p / u_e is exactly half-way between two integers (the result then
-// depends on the parity of the sum).  `big` is set when the step count does
-// not fit the binade (p itself reaches 2^(e+1)).
-template <class A>
-QSLC_HD uint64_t grid_steps(A p, int e, bool &tie, bool &big)
+// of type A lying in binade e: rne(p / u_e) with u_e = 2^(e - MANT of A).
+// `tie` is set when p / u_e is exactly half-way between two integers (the
+// result then depends on the parity of the sum).  `big` is set when the
+// step count does not fit the binade (p itself reaches 2^(e+1)).  The term
+// may be of another type P (a float term held as a double, say): its value
+// is decoded from its own format.
+template <class A, class P = A>
+QSLC_HD uint64_t grid_steps(P p, int e, bool &tie, bool &big)
 {
     using T = fp_traits<A>;
+    using TP = fp_traits<P>;
     tie = false;
     big = false;
     auto b = to_bits(p);
-    int ef = int((b >> T::MANT) & T::EXPMASK);
-    uint64_t m = uint64_t(b & ((typename T::bits_t(1) << T::MANT) - 1));
+    int ef = int((b >> TP::MANT) & TP::EXPMASK);
+    uint64_t m = uint64_t(b & ((typename TP::bits_t(1) << TP::MANT) - 1));
     if (ef == 0 && m == 0) return 0;
     int lsb;                                  // exponent of m's last bit
     if (ef != 0) {
-        m |= uint64_t(1) << T::MANT;
-        lsb = ef - T::BIAS - T::MANT;
+        m |= uint64_t(1) << TP::MANT;
+        lsb = ef - TP::BIAS - TP::MANT;
     } else {
-        lsb = T::EMIN - T::MANT;
+        lsb = TP::EMIN - TP::MANT;
     }
     int sh = (e - T::MANT) - lsb;             // p / u_e = m * 2^-sh
     if (sh <= 0) {
@@ -102,6 +105,8 @@ QSLC_HD uint64_t grid_steps(A p, int e, bool &tie, bool &big)
         if (ls > T::MANT + 1 || (m >> (T::MANT + 1 - ls)) != 0) { big = true; return 0; }
         return m << ls;
     }
+    // a term of more precision than the sum: its step count may not fit
+    if (T::MANT + 1 + sh < 64 && (m >> (T::MANT + 1 + sh)) != 0) { big = true; return 0; }
     if (sh >= 64) return 0;                   // m < 2^53 <= half a step
     uint64_t q = m >> sh;
     uint64_t rem = m & ((uint64_t(1) << sh) - 1);
@@ -171,34 +176,34 @@ QSLC_HD uint64_t grid_ceil(A u, int e)
     return q + ((m & ((uint64_t(1) << sh) - 1)) != 0 ? 1 : 0);
 }
 
-// Runs of consecutive terms of a running sum in binade e, for walking a
-// sampling CDF a warp at a time: each lane takes one run, run_effect gives
-// the run's Tx (composed across lanes by a scan), run_walk advances a grid
-// position through the run from where the lanes before left it, and
-// run_find locates the term at which the position reaches a uniform's
-// target.  The position must stay below 2^(MANT+1) (the binade's end);
-// run_walk stops before the first term that would take it there, or whose
-// step count does not fit the binade.
-template <class A>
-QSLC_HD Tx run_effect(const A *p, unsigned len, int e, bool &big_any)
+// Runs of consecutive terms of a running sum of type A in binade e, for
+// walking a sequential sum a warp at a time: each lane takes one run (its
+// terms get(0), get(1), ...), run_effect gives the run's Tx (composed across
+// lanes by a scan), run_walk advances a grid position through the run from
+// where the lanes before left it, and run_find locates the term at which
+// the position reaches a target.  The position must stay below 2^(MANT+1)
+// (the binade's end); run_walk stops before the first term that would take
+// it there, or whose step count does not fit the binade.
+template <class A, class Get>
+QSLC_HD Tx run_effect(Get get, unsigned len, int e, bool &big_any)
 {
     Tx t = tx_identity();
     for (unsigned r = 0; r < len; r++) {
         bool tie, big;
-        const uint64_t q = grid_steps<A>(p[r], e, tie, big);
+        const uint64_t q = grid_steps<A>(get(r), e, tie, big);
         big_any |= big;
         t = tx_then(t, tx_term(q, tie));
     }
     return t;
 }
 
-template <class A>
-QSLC_HD unsigned run_walk(const A *p, unsigned len, int e, uint64_t &pos)
+template <class A, class Get>
+QSLC_HD unsigned run_walk(Get get, unsigned len, int e, uint64_t &pos)
 {
     const uint64_t lim = uint64_t(1) << (fp_traits<A>::MANT + 1);
     for (unsigned r = 0; r < len; r++) {
         bool tie, big;
-        const uint64_t q = grid_steps<A>(p[r], e, tie, big);
+        const uint64_t q = grid_steps<A>(get(r), e, tie, big);
         if (big || pos >= lim) return r;
         const uint64_t step = tx_term(q, tie).d[pos & 1];
         if (step >= lim - pos) return r;
@@ -207,16 +212,42 @@ QSLC_HD unsigned run_walk(const A *p, unsigned len, int e, uint64_t &pos)
     return len;
 }
 
-template <class A>
-QSLC_HD unsigned run_find(const A *p, unsigned len, int e, uint64_t pos, uint64_t target)
+template <class A, class Get>
+QSLC_HD unsigned run_find(Get get, unsigned len, int e, uint64_t pos, uint64_t target)
 {
     for (unsigned r = 0; r < len; r++) {
         bool tie, big;
-        const uint64_t q = grid_steps<A>(p[r], e, tie, big);
+        const uint64_t q = grid_steps<A>(get(r), e, tie, big);
         pos += tx_term(q, tie).d[pos & 1];
         if (pos >= target) return r;
     }
     return len;
+}
+
+// The value of type A at grid position `pos` of binade e (pos in
+// [2^MANT, 2^(MANT+1))).
+template <class A>
+QSLC_HD A grid_at(uint64_t pos, int e)
+{
+    using T = fp_traits<A>;
+    const auto b = typename T::bits_t((uint64_t(e + T::BIAS) << T::MANT) | (pos - (uint64_t(1) << T::MANT)));
+    A x;
+#ifdef __CUDA_ARCH__
+    if constexpr (sizeof(A) == 8) x = __longlong_as_double((long long)b);
+    else x = __uint_as_float(uint32_t(b));
+#else
+    std::memcpy(&x, &b, sizeof(A));
+#endif
+    return x;
+}
+
+// The grid position of a normal x of type A in its binade: its significand
+// with the hidden bit.
+template <class A>
+QSLC_HD uint64_t grid_pos(A x)
+{
+    using T = fp_traits<A>;
+    return (uint64_t(to_bits(x)) & ((uint64_t(1) << T::MANT) - 1)) | (uint64_t(1) << T::MANT);
 }
 
 // |a|^2 as the reference computes it: RN(RN(re*re) + RN(im*im))

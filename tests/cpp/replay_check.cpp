@@ -110,27 +110,36 @@ static std::vector<uint64_t> cdf_sequential(const std::vector<double> &p, const 
     return out;
 }
 
-// The batching form's CDF walk (k_batch_cdf in batch.cu), its 32 lanes
+// The batching form's warp walk (warp_walk in batch.cu), its 32 lanes
 // emulated one after another: rounds of 32 runs of `run` terms in one
 // binade, a scan of the runs' transducers, the walks, the first term that
 // leaves the binade added on its own; zero sums skip zero terms 32 at a
-// time, subnormal sums add one term at a time.
-static std::vector<uint64_t> cdf_rounds(const std::vector<double> &p, const std::vector<double> &u,
-                                        unsigned run)
+// time, subnormal sums add one term at a time.  A is the sum's type (the
+// terms are doubles); with uniforms, the sum is a CDF and each uniform's
+// outcome goes to `out`.
+template <class A>
+static A add_term(A s, double t)
+{
+    volatile A r = s + A(t);
+    return r;
+}
+
+template <class A>
+static A walk_rounds(const std::vector<double> &p, const std::vector<double> *u, std::vector<uint64_t> *out,
+                     unsigned run)
 {
     const uint64_t dim = p.size(), NONE = ~uint64_t(0);
-    const size_t ns = u.size();
-    std::vector<uint64_t> out(ns, 0);
+    const size_t ns = u ? u->size() : 0;
     size_t k = 0;
-    double s = 0;
+    A s = 0;
     uint64_t i = 0;
     auto consume = [&](uint64_t idx) {
-        while (k < ns && bits_of(u[k]) <= bits_of(s)) out[k++] = idx;
+        while (k < ns && bits_of((*u)[k]) <= bits_of(double(s))) (*out)[k++] = idx;
     };
-    while (i < dim && k < ns) {
-        const int e = binade<double>(s);
-        if (e < fp_traits<double>::EMIN) {
-            if (bits_of(s) == 0) {
+    while (i < dim && (!u || k < ns)) {
+        const int e = binade<A>(s);
+        if (e < fp_traits<A>::EMIN) {
+            if (to_bits(s) == 0) {
                 unsigned first = 32;
                 for (unsigned l = 0; l < 32; l++)
                     if (i + l < dim && bits_of(p[i + l]) != 0) {
@@ -144,13 +153,12 @@ static std::vector<uint64_t> cdf_rounds(const std::vector<double> &p, const std:
                 }
                 i += first;
             }
-            volatile double nx = s + p[i];
-            s = nx;
+            s = add_term(s, p[i]);
             consume(i);
             i++;
             continue;
         }
-        const uint64_t m0 = (bits_of(s) & ((uint64_t(1) << 52) - 1)) | (uint64_t(1) << 52);
+        const uint64_t m0 = grid_pos(s);
         const uint64_t end = i + 32 * run < dim ? i + 32 * run : dim;
         uint64_t base[32], pos0[32], pos[32];
         unsigned len[32];
@@ -159,19 +167,21 @@ static std::vector<uint64_t> cdf_rounds(const std::vector<double> &p, const std:
         for (unsigned l = 0; l < 32; l++) {
             base[l] = i + uint64_t(l) * run;
             len[l] = base[l] < end ? unsigned(end - base[l] < run ? end - base[l] : run) : 0u;
+            const double *pl = p.data() + base[l];
+            auto get = [pl](unsigned r) { return pl[r]; };
             bool big = false;
-            const Tx t = run_effect<double>(p.data() + base[l], len[l], e, big);
+            const Tx t = run_effect<A>(get, len[l], e, big);
             pos0[l] = m0 + acc.d[m0 & 1];
             acc = tx_then(acc, t);
             pos[l] = pos0[l];
-            const unsigned walked = run_walk<double>(p.data() + base[l], len[l], e, pos[l]);
+            const unsigned walked = run_walk<A>(get, len[l], e, pos[l]);
             if (walked < len[l] && base[l] + walked < bad) bad = base[l] + walked;
         }
         const uint64_t stop = bad == NONE ? end : bad;
         const uint64_t last = bad == NONE ? end - 1 : stop;
         const uint64_t pend = pos[(last - i) / run];
         while (k < ns) {
-            const uint64_t tgt = grid_ceil<double>(u[k], e);
+            const uint64_t tgt = grid_ceil<A>(A((*u)[k]), e);
             if (tgt > pend) break;
             unsigned L = 32;
             for (unsigned l = 0; l < 32; l++)
@@ -180,19 +190,61 @@ static std::vector<uint64_t> cdf_rounds(const std::vector<double> &p, const std:
                     break;
                 }
             if (L == 32) break;
-            out[k++] = base[L] + run_find<double>(p.data() + base[L], len[L], e, pos0[L], tgt);
+            const double *pL = p.data() + base[L];
+            (*out)[k++] = base[L] + run_find<A>([pL](unsigned r) { return pL[r]; }, len[L], e, pos0[L], tgt);
         }
-        const uint64_t sb = (uint64_t(e + 1023) << 52) | (pend - (uint64_t(1) << 52));
-        std::memcpy(&s, &sb, 8);
+        s = grid_at<A>(pend, e);
         i = stop;
         if (bad != NONE) {
-            volatile double nx = s + p[i];
-            s = nx;
+            s = add_term(s, p[i]);
             consume(i);
             i++;
         }
     }
+    return s;
+}
+
+static std::vector<uint64_t> cdf_rounds(const std::vector<double> &p, const std::vector<double> &u,
+                                        unsigned run)
+{
+    std::vector<uint64_t> out(u.size(), 0);
+    walk_rounds<double>(p, &u, &out, run);
     return out;
+}
+
+// Probability-like sums: the walk's total against the sequential sum, in
+// double, and in float over float terms (held as doubles).
+static int check_sums(int trials)
+{
+    int fails = 0, cases = 0;
+    for (int t = 0; t < trials; t++) {
+        const uint64_t dim = 1 + rng() % 20000;
+        std::vector<double> p(dim);
+        std::normal_distribution<double> g;
+        const int kind = int(rng() % 4);
+        for (auto &x : p) {
+            const double re = g(rng), im = g(rng);
+            x = std::ldexp(re * re + im * im, -int(rng() % 3) - 14);
+            if (kind == 1 && rng() % 3 == 0) x = 0;
+            if (kind == 2) x = std::ldexp(1.0, -14);
+            if (kind == 3) x = std::ldexp(double(rng() % 5), -149);        // float subnormals
+        }
+        double sd = 0;
+        for (double x : p) sd = add_term(sd, x);
+        std::vector<double> pf(p.begin(), p.end());
+        for (auto &x : pf) x = double(float(x));
+        float sf = 0;
+        for (double x : pf) sf = add_term(sf, x);
+        for (unsigned r : {1u, 16u}) {
+            cases += 2;
+            const double gd = walk_rounds<double>(p, nullptr, nullptr, r);
+            const float gf = walk_rounds<float>(pf, nullptr, nullptr, r);
+            if (bits_of(gd) != bits_of(sd) && fails++ < 5) std::printf("double sum differs: kind %d\n", kind);
+            if (to_bits(gf) != to_bits(sf) && fails++ < 5) std::printf("float sum differs: kind %d\n", kind);
+        }
+    }
+    std::printf("sums: %d cases, %d fails\n", cases, fails);
+    return fails;
 }
 
 // Term sequences that exercise every path of the walk: |a|^2 of random
@@ -257,6 +309,7 @@ int main()
     int f = check<double, double>(3000) + check<double, float>(3000) + check<float, float>(3000);
     f += check_ceil(200000);
     f += check_cdf_walk(1500);
+    f += check_sums(600);
     if (f) return 1;
     std::puts("replay ok");
     return 0;
