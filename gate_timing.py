@@ -12,7 +12,13 @@ timed gate:
 
     python gate_timing.py [--qubits 26] [--gates hadamard,rotateX,hadamard,rotateX]
                           [--targets 3,9,15,21] [--pairs 0:5,5:0,20:21] [--angle 0.4]
-                          [--repeat 1]
+                          [--repeat 1] [--grouped]
+
+Each gate runs alone (the library's grouping of consecutive one-qubit
+gates is switched off, QSLC_GROUP=0).  With --grouped, grouping stays on
+and each timed window holds two one-qubit gates, on target t and on
+target t + 1 (mod n), which run as one sweep; the rate is then the two
+gates' algorithmic bytes over the window's time.
 
 A gate on a state of zeros or of few nonzero amplitudes runs faster
 than on a dense one (operands that are zero take a shorter path through
@@ -62,7 +68,7 @@ def parse_pairs(text: str, n: int):
     return pairs
 
 
-def run(qubits: int, gates, targets, pairs, angle: float, repeat: int = 1) -> dict:
+def run(qubits: int, gates, targets, pairs, angle: float, repeat: int = 1, grouped: bool = False) -> dict:
     import torch
 
     from qsl_gb300 import Qubits
@@ -71,10 +77,13 @@ def run(qubits: int, gates, targets, pairs, angle: float, repeat: int = 1) -> di
     sim = Qubits(qubits)
     sim.set_stream(stream.cuda_stream)
     prepare_dense(sim, qubits)
+    sim.flush()
     torch.cuda.synchronize()
     out = {}
     for name in gates:
-        where = [(t, None) for t in targets] if name in ONE_QUBIT_AMPS else pairs
+        one = name in ONE_QUBIT_AMPS
+        where = [(t, None) for t in targets] if one else pairs
+        pair = grouped and one
         times = []
         for q1, q2 in where:
             best = None
@@ -83,12 +92,16 @@ def run(qubits: int, gates, targets, pairs, angle: float, repeat: int = 1) -> di
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
                 sim.gate(name, q1, q2, angle)
+                if pair:
+                    sim.gate(name, (q1 + 1) % qubits, None, angle)
+                sim.flush()
                 e1.record(stream)
                 torch.cuda.synchronize()
                 us = e0.elapsed_time(e1) * 1e3
                 best = us if best is None else min(best, us)
             times.append(round(best, 1))
-        gbs = [round(alg_bytes(name, qubits) / (us * 1e-6) / 1e9) for us in times]
+        nb = alg_bytes(name, qubits) * (2 if pair else 1)
+        gbs = [round(nb / (us * 1e-6) / 1e9) for us in times]
         out.setdefault(name, []).append({"us": times, "gbs": gbs, "where": where})
         print(name, where, times, "us", gbs, "GB/s", flush=True)
     return out
@@ -102,6 +115,8 @@ def main(argv=None) -> None:
     ap.add_argument("--pairs", default="0:5,5:0,1:9,20:21")
     ap.add_argument("--angle", type=float, default=0.4)
     ap.add_argument("--repeat", type=int, default=1)
+    ap.add_argument("--grouped", action="store_true",
+                    help="time one-qubit gates two to a window, grouped into one sweep")
     a = ap.parse_args(argv)
     targets = [int(t) for t in a.targets.split(",")]
     if any(t < 0 or t >= a.qubits for t in targets):
@@ -114,7 +129,9 @@ def main(argv=None) -> None:
     for g in gates:
         if g not in ONE_QUBIT_AMPS and g not in TWO_QUBIT_AMPS:
             ap.error(f"unknown gate {g}")
-    run(a.qubits, gates, targets, pairs, a.angle, max(1, a.repeat))
+    if not a.grouped:
+        os.environ["QSLC_GROUP"] = "0"         # read once, at the library's first gate
+    run(a.qubits, gates, targets, pairs, a.angle, max(1, a.repeat), a.grouped)
 
 
 if __name__ == "__main__":

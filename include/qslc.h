@@ -139,7 +139,12 @@ QSLC_API int qslc_get_state(const qslc_state *s, void *amps, uint64_t n_amps);
 QSLC_API int qslc_set_basis(qslc_state *s, uint64_t index);
 
 /* One-qubit gate: pauliX, ..., rotateZ (gates.cpp:32-209; np/gates.cpp:33-113).
- * `angle` is ignored by the gates without one. */
+ * `angle` is ignored by the gates without one.  On a plain state the gate
+ * may be held back until the handle's next call: a one-qubit gate on
+ * another qubit then runs with it in one sweep, with the same bits as two;
+ * any other call applies it first.  qslc_flush or qslc_synchronize apply a
+ * held gate without another call; QSLC_GROUP=0 in the environment turns
+ * the holding off. */
 QSLC_API int qslc_gate1(qslc_state *s, int gate, unsigned targ, double angle);
 
 /* Two-qubit gate (gates.cpp:215-682; np/gates.cpp:118-415).  EINVAL when

@@ -159,10 +159,21 @@ int check_handle(const qslc_state *s)
     return QSLC_OK;
 }
 
-// Apply queued gates of the precision form before the state is read, and
-// report a staged sweep whose barrier wait ran out since the last check.
+// Launch the one-qubit gate held back for grouping, alone.
+int release_held(qslc_state *s)
+{
+    if (!s->has_held) return QSLC_OK;
+    s->has_held = false;
+    return launch_gate1(s, s->held.code, s->held.q1, s->held.angle);
+}
+
+// Apply held and queued gates (the gate held for grouping; the precision
+// form's queue) before the state is read, and report a staged sweep whose
+// barrier wait ran out since the last check.
 int flushed(qslc_state *s)
 {
+    int hrc = release_held(s);
+    if (hrc) return hrc;
     if (!s->fuse_queue.empty()) {
         int rc = fusion_flush(s);
         if (rc) return rc;
@@ -394,6 +405,7 @@ int qslc_assign(qslc_state *dst, const qslc_state *src)
     rc = flushed(const_cast<qslc_state *>(src));
     if (rc) return rc;
     dst->fuse_queue.clear();                 // overwritten below
+    dst->has_held = false;
     if (dst->resizable && dst->namps != src->namps) {
         rc = resize_capacity(dst, src->namps);
         if (rc) return rc;
@@ -442,6 +454,7 @@ int qslc_reset(qslc_state *s)
     int rc = check_handle(s);
     if (rc) return rc;
     s->fuse_queue.clear();
+    s->has_held = false;
     return launch_fill_basis(s, 0);
 }
 
@@ -464,6 +477,7 @@ int qslc_set_state(qslc_state *s, const void *amps, uint64_t n_amps)
     if (n_amps != dim)
         return fail(QSLC_ESIZE, "Cannot assign state vector from different number of qubits");
     s->fuse_queue.clear();
+    s->has_held = false;
     if (!s->np) {
         QSLC_CUDA(cudaMemcpyAsync(s->amps, amps, dim * s->amp_bytes(), cudaMemcpyHostToDevice, s->stream));
         QSLC_CUDA(cudaStreamSynchronize(s->stream));
@@ -504,6 +518,7 @@ int qslc_set_basis(qslc_state *s, uint64_t index)
     if (s->n < 64 && index >= (uint64_t(1) << s->n))
         return fail(QSLC_EINVAL, "basis index out of range");
     s->fuse_queue.clear();
+    s->has_held = false;
     if (!s->np) return launch_fill_basis(s, index);
     const unsigned w = unsigned(__builtin_popcountll(index));
     if (w != s->nones) {
@@ -531,7 +546,19 @@ int qslc_gate1(qslc_state *s, int gate, unsigned targ, double angle)
         s->fuse_queue.push_back(GateOp{gate, targ, targ, angle});
         return QSLC_OK;
     }
-    return launch_gate1(s, gate, targ, angle);
+    if (!grouping_enabled()) return launch_gate1(s, gate, targ, angle);
+    // one-qubit gates on different qubits run two to a sweep: hold this
+    // one until the next call, which either joins it or releases it
+    const GateOp g{gate, targ, targ, angle};
+    if (s->has_held) {
+        s->has_held = false;
+        if (s->held.q1 != targ) return launch_group2(s, s->held, g);
+        rc = launch_gate1(s, s->held.code, s->held.q1, s->held.angle);
+        if (rc) return rc;
+    }
+    s->held = g;
+    s->has_held = true;
+    return QSLC_OK;
 }
 
 int qslc_gate2(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle)
@@ -554,6 +581,8 @@ int qslc_gate2(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle)
         s->fuse_queue.push_back(GateOp{gate, q1, q2, angle});
         return QSLC_OK;
     }
+    rc = release_held(s);
+    if (rc) return rc;
     return launch_gate2(s, gate, q1, q2, angle);
 }
 

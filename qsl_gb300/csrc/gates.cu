@@ -181,6 +181,99 @@ __global__ void QSLC_SWEEP_BOUNDS k_diag1(cplx<T> *__restrict__ st, uint64_t cou
     }
 }
 
+// Two one-qubit gates on different qubits in one sweep (gate grouping).
+// A thread holds the four amplitudes that differ only in the two target
+// bits, applies the first gate to its two pairs along the first gate's bit
+// and then the second gate to its two pairs along the other bit.  Every
+// amplitude sees the same operations, in the same order, as in two
+// sweeps, so the bits are those of the two gates one after the other; the
+// state is read and written once instead of twice.
+//
+// `op` is a PairOp, or GROUP_DIAG + a DiagOp for phase and pauliZ (which
+// act on the members with the bit set).  The output modes (gatemath.cuh)
+// are fixed per gate type: the two pair updates of a rotation take the
+// low and high byte of QSLC_GROUP_MODES_ROT, and so on.
+constexpr int GROUP_DIAG = 16;
+#ifndef QSLC_GROUP_MODES_ROT
+#define QSLC_GROUP_MODES_ROT 0x1595u      // PPPQ, PPPF
+#endif
+#ifndef QSLC_GROUP_MODES_H
+#define QSLC_GROUP_MODES_H 0x0000u        // FFFF, FFFF
+#endif
+#ifndef QSLC_GROUP_MODES_DIAG
+#define QSLC_GROUP_MODES_DIAG 0x0509u     // PQ, PP
+#endif
+
+template <class T>
+struct GroupGates {
+    int op[2];
+    Coef<T> k[2];
+};
+
+// One gate of a group on the pairs (x0, x1) and (y0, y1); x1 and y1 are
+// the members with the gate's bit set.
+template <class T>
+__device__ __forceinline__ void group_apply(int op, cplx<T> &x0, cplx<T> &x1, cplx<T> &y0, cplx<T> &y1,
+                                            const Coef<T> &k)
+{
+    constexpr unsigned R0 = QSLC_GROUP_MODES_ROT & 0xFFu, R1 = (QSLC_GROUP_MODES_ROT >> 8) & 0xFFu;
+    constexpr unsigned H0 = QSLC_GROUP_MODES_H & 0xFFu, H1 = (QSLC_GROUP_MODES_H >> 8) & 0xFFu;
+    constexpr unsigned D0 = QSLC_GROUP_MODES_DIAG & 0xFFu, D1 = (QSLC_GROUP_MODES_DIAG >> 8) & 0xFFu;
+    switch (op) {
+    case P_SWAP:
+        pair_update<T, P_SWAP>(x0, x1, k);
+        pair_update<T, P_SWAP>(y0, y1, k);
+        break;
+    case P_Y:
+        pair_update<T, P_Y>(x0, x1, k);
+        pair_update<T, P_Y>(y0, y1, k);
+        break;
+    case P_H:
+        pair_update<T, P_H>(x0, x1, k, H0);
+        pair_update<T, P_H>(y0, y1, k, H1);
+        break;
+    case P_RX:
+        pair_update<T, P_RX>(x0, x1, k, R0);
+        pair_update<T, P_RX>(y0, y1, k, R1);
+        break;
+    case P_RY:
+        pair_update<T, P_RY>(x0, x1, k, R0);
+        pair_update<T, P_RY>(y0, y1, k, R1);
+        break;
+    case P_RZ:
+        pair_update<T, P_RZ>(x0, x1, k, R0);
+        pair_update<T, P_RZ>(y0, y1, k, R1);
+        break;
+    case GROUP_DIAG + D_NEG:
+        diag_update<T, D_NEG>(x1, k);
+        diag_update<T, D_NEG>(y1, k);
+        break;
+    default:                                  // GROUP_DIAG + D_PHASE
+        diag_update<T, D_PHASE>(x1, k, D0);
+        diag_update<T, D_PHASE>(y1, k, D1);
+        break;
+    }
+}
+
+// quads j in [0, 2^(n-2)): x = j with zeros inserted at bits lo < hi; the
+// first gate acts on bit mask c0, the second on c1 ({c0, c1} = {2^lo, 2^hi}).
+template <class T, class IX = uint64_t>
+__global__ void QSLC_SWEEP_BOUNDS k_group2(cplx<T> *__restrict__ st, uint64_t nquads, unsigned lo, unsigned hi,
+                                                IX c0, IX c1, GroupGates<T> g)
+{
+    const IX stride = IX(gridDim.x) * blockDim.x;
+    for (IX j = IX(blockIdx.x) * blockDim.x + threadIdx.x; j < IX(nquads); j += stride) {
+        const IX x = ins00<IX>(j, lo, hi);
+        cplx<T> a00 = st[x], a01 = st[x | c0], a10 = st[x | c1], a11 = st[x | c0 | c1];
+        group_apply<T>(g.op[0], a00, a01, a10, a11, g.k[0]);
+        group_apply<T>(g.op[1], a00, a10, a01, a11, g.k[1]);
+        st[x] = a00;
+        st[x | c0] = a01;
+        st[x | c1] = a10;
+        st[x | c0 | c1] = a11;
+    }
+}
+
 // rotateZ touches both halves with different coefficients; it is a pair
 // gate whose two members do not mix (gates.cpp:181-209).
 
@@ -731,7 +824,58 @@ int gate2_t(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle)
     return QSLC_OK;
 }
 
+// A plain one-qubit gate as a group member: its op and coefficients.
+template <class T>
+void group_member(const GateOp &g, int &op, Coef<T> &k)
+{
+    k = Coef<T>{};
+    switch (g.code) {
+    case QSLC_PAULI_X: op = P_SWAP; break;
+    case QSLC_PAULI_Y: op = P_Y; break;
+    case QSLC_PAULI_Z: op = GROUP_DIAG + D_NEG; break;
+    case QSLC_HADAMARD: op = P_H; k = sqrt2_coef<T>(); break;
+    case QSLC_PHASE: op = GROUP_DIAG + D_PHASE; k = full_angle<T>(g.angle); break;
+    case QSLC_ROTATE_X: op = P_RX; k = half_angle<T>(g.angle); break;
+    case QSLC_ROTATE_Y: op = P_RY; k = half_angle<T>(g.angle); break;
+    default: op = P_RZ; k = half_angle<T>(g.angle); break;
+    }
+}
+
+template <class T>
+int group2_t(qslc_state *s, const GateOp &g0, const GateOp &g1)
+{
+    GroupGates<T> g;
+    group_member<T>(g0, g.op[0], g.k[0]);
+    group_member<T>(g1, g.op[1], g.k[1]);
+    const unsigned lo = g0.q1 < g1.q1 ? g0.q1 : g1.q1, hi = g0.q1 < g1.q1 ? g1.q1 : g0.q1;
+    const uint64_t quads = uint64_t(1) << (s->n - 2);
+    auto *st = static_cast<cplx<T> *>(s->amps);
+    with_index(s->n, [&](auto ix) {
+        using IX = decltype(ix);
+        k_group2<T, IX><<<grid_for(quads), 256, 0, s->stream>>>(st, quads, lo, hi, IX(1) << g0.q1,
+                                                               IX(1) << g1.q1, g);
+    });
+    s->launches++;
+    QSLC_CUDA(cudaGetLastError());
+    return QSLC_OK;
+}
+
 }  // namespace
+
+// Grouping is on unless QSLC_GROUP=0.
+bool grouping_enabled()
+{
+    static const bool on = [] {
+        const char *e = std::getenv("QSLC_GROUP");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
+int launch_group2(qslc_state *s, const GateOp &g0, const GateOp &g1)
+{
+    return s->dtype == QSLC_C128 ? group2_t<double>(s, g0, g1) : group2_t<float>(s, g0, g1);
+}
 
 int launch_gate1(qslc_state *s, int gate, unsigned targ, double angle)
 {

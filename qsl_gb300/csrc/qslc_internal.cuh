@@ -140,6 +140,10 @@ struct qslc_state {
     qslc::Scratch fuse_mats;
     qslc::Scratch fuse_tc_mats;   // packed tensor-core operands, then an error word
     uint64_t fused_blocks = 0;
+    // a one-qubit gate held back to run in one sweep with the next
+    // one-qubit gate on another qubit (gates.cu, k_group2)
+    qslc::GateOp held{};
+    bool has_held = false;
     int *wait_err = nullptr;         // device word set by a staged sweep whose barrier wait ran out
     bool wait_err_pending = false;   // staged sweeps launched since the word was last read
 
@@ -170,6 +174,9 @@ int wait_error(qslc_state *s);
 // gates.cu
 int launch_gate1(qslc_state *s, int gate, unsigned targ, double angle);
 int launch_gate2(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle);
+// two one-qubit gates on different qubits, in this order, in one sweep
+int launch_group2(qslc_state *s, const GateOp &g0, const GateOp &g1);
+bool grouping_enabled();
 int launch_collapse(qslc_state *s, unsigned targ, unsigned outcome, double factor);
 // complex64 collapse with the factor applied in double (precision form)
 int launch_collapse_f64(qslc_state *s, unsigned targ, unsigned outcome, double factor);
