@@ -496,6 +496,38 @@ def e2e_pinned(n, local_ranks):
     return local_ranks * (1 << n) * 16 <= ram // 2
 
 
+def launch_windows(layer, grouping=True):
+    """The calls of one layer with the gates of the kernel each launches.
+
+    The library holds a one-qubit gate back until the next call: a
+    one-qubit gate on another qubit joins it in one sweep (k_group2),
+    anything else releases it alone.  Before a two-qubit gate, and at the
+    end of the layer, a held gate is released by an explicit flush (call
+    None), so each timing window holds one kernel.  Returns (call, gates)
+    pairs; gates is None for a call that launches nothing."""
+    out, held = [], None
+    for g, a, b, x in layer:
+        gate = (g, a, b, x)
+        if b is None and grouping:
+            if held is None:
+                out.append((gate, None))
+                held = gate
+            elif held[1] != a:
+                out.append((gate, [held, gate]))
+                held = None
+            else:
+                out.append((gate, [held]))
+                held = gate
+            continue
+        if held is not None:
+            out.append((None, [held]))
+            held = None
+        out.append((gate, [gate]))
+    if held is not None:
+        out.append((None, [held]))
+    return out
+
+
 def roofline_of(args, name, top, peak, peak_kind):
     """The roofline object of the dominant kernel: its algorithmic bytes per
     launch (the reference's count, 2 x 16 B x amplitudes changed, for every
@@ -556,31 +588,11 @@ def run_gpu(args):
             timing.append((launched, e0, e1))
 
     def run_layer(li, timing):
-        # The library holds a one-qubit gate back until the next call: a
-        # one-qubit gate on another qubit joins it in one sweep (k_group2),
-        # anything else releases it alone.  The windows follow the launches:
-        # the held gate is released by an explicit flush before a two-qubit
-        # gate, so each window holds one kernel.
-        held = None
-        for g, a, b, x in layers[li % len(layers)]:
-            if b is None and grouping:
-                if held is None:
-                    launched = None
-                elif held[1] != a:
-                    launched = [held, (g, a, b, x)]
-                else:
-                    launched = [held]
-                held = (g, a, b, x)
-                if launched and len(launched) == 2:
-                    held = None
-                timed(timing, lambda: sim.gate(g, a, b, x), launched)
-                continue
-            if held is not None:
-                timed(timing, sim.flush, [held])
-                held = None
-            timed(timing, lambda: sim.gate(g, a, b, x), [(g, a, b, x)])
-        if held is not None:
-            timed(timing, sim.flush, [held])
+        for call, launched in launch_windows(layers[li % len(layers)], grouping):
+            if call is None:
+                timed(timing, sim.flush, launched)
+            else:
+                timed(timing, lambda: sim.gate(*call), launched)
 
     # warm-up layers (the circuit's own first layers)
     for w in range(args.warmup):

@@ -74,3 +74,20 @@ def test_bench_relaunches_itself_only_without_a_launcher(monkeypatch):
     monkeypatch.setenv("WORLD_SIZE", "4")
     bench.main()
     assert calls == ["gpu"]
+
+
+def test_launch_windows_follow_the_grouping():
+    """The bench's timing windows mirror the library's grouping: a held
+    one-qubit gate joins the next one on another qubit, is released alone
+    by a gate on the same qubit, and by an explicit flush before a
+    two-qubit gate and at the end of a layer."""
+    import bench
+    ry0, rz1, h2, p2, h3 = (("rotateY", 0, None, .1), ("rotateZ", 1, None, .2), ("hadamard", 2, None, 0.),
+                            ("phase", 2, None, .3), ("hadamard", 3, None, 0.))
+    cx = ("controlNot", 0, 1, 0.)
+    w = bench.launch_windows([ry0, rz1, h2, p2, cx, h3])
+    assert w == [(ry0, None), (rz1, [ry0, rz1]), (h2, None), (p2, [h2]), (None, [p2]), (cx, [cx]),
+                 (h3, None), (None, [h3])]
+    assert bench.launch_windows([ry0, rz1], grouping=False) == [(ry0, [ry0]), (rz1, [rz1])]
+    launched = [g for _, gs in w if gs for g in gs]
+    assert launched == [ry0, rz1, h2, p2, cx, h3]
