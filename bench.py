@@ -83,6 +83,9 @@ def kernel_of(gate: str) -> str:
 # amplitude count).  It is not measured by this program: the JSON line says
 # so next to the number, and --traffic replaces it with a capture's figure.
 K_PAIR1_TRAFFIC_RATIO = 2.086 / 2.147
+# The same for the grouped sweep of two rotations on a dense 26-qubit state:
+# 1.074 + 1.012 GB of DRAM traffic for the two gates' 2 x 2.147 GB.
+K_GROUP2_TRAFFIC_RATIO = (1.074 + 1.012) / (2 * 2.147)
 
 
 def peaks():
@@ -550,6 +553,11 @@ def roofline_of(args, name, top, peak, peak_kind):
         out["traffic"] = per_launch * K_PAIR1_TRAFFIC_RATIO
         out["traffic_source"] = ("scaled from an earlier ncu capture of k_pair1 on a dense 26-qubit "
                                  "state (DRAM bytes / algorithmic bytes = 0.972); not measured in this run")
+    elif name == "k_group2":
+        out["traffic"] = per_launch * K_GROUP2_TRAFFIC_RATIO
+        out["traffic_source"] = ("scaled from an earlier ncu capture of k_group2 (two rotations) on a dense "
+                                 "26-qubit state (DRAM bytes / algorithmic bytes of both gates = 0.486: one "
+                                 "read and one write of the state); not measured in this run")
     else:
         out["traffic"] = None
         out["traffic_source"] = "no capture of this kernel given"
