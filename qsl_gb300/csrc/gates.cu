@@ -1,5 +1,10 @@
 // gates.cu -- amplitude-pair sweeps of the plain (2^n) layout.
 //
+// The sweeps: k_pair1 / k_diag1 / k_pair2 / k_diag2, one gate per sweep
+// from registers; k_group2, two one-qubit gates on different qubits in one
+// sweep; k_pair1_shfl, pairs inside a warp exchanged between lanes; and
+// the staged sweeps through shared memory (opt-in, stage.cuh).
+//
 // One thread owns one amplitude pair (or one amplitude for the diagonal
 // gates) in a grid-stride loop.  The pair index j is turned into the basis
 // index by inserting the target bit (bit insertion replaces the reference's
