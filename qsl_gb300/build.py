@@ -64,7 +64,7 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
         objs = list(ex.map(lambda s: _compile(s, extra), srcs))
     cudalib = os.path.join(os.path.dirname(os.path.dirname(nvcc())), "lib64")
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-L", cudalib,
+    cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread", "-L", cudalib,
            "-Xlinker", "-rpath", "-Xlinker", cudalib]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -42,6 +42,7 @@
 #include <algorithm>
 #include <cmath>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 namespace qslc {
@@ -670,6 +671,27 @@ int capture_any(qslc_batch *b, const BatchShape &s)
     return b->dtype == QSLC_C128 ? capture<double>(b, s) : capture<float>(b, s);
 }
 
+// f(i) for every i in [0, n) on the host's cores: instance i goes to thread
+// i mod T, so instances of every size spread over the threads.  Each f(i)
+// touches only instance i's data.
+template <class F>
+void host_parallel(uint32_t n, F &&f)
+{
+    unsigned nt = std::thread::hardware_concurrency();
+    nt = std::min<unsigned>(std::max<unsigned>(nt, 1u), 32u);
+    if (nt < 2 || n < 256) {
+        for (uint32_t i = 0; i < n; i++) f(i);
+        return;
+    }
+    std::vector<std::thread> pool;
+    pool.reserve(nt);
+    for (unsigned t = 0; t < nt; t++)
+        pool.emplace_back([&f, n, nt, t] {
+            for (uint32_t i = t; i < n; i += nt) f(i);
+        });
+    for (auto &th : pool) th.join();
+}
+
 // Coefficients exactly as the reference computes them (gates.cpp:154-155,
 // :185-186: Fp cos/sin of Fp(angle)/2) and each instance's uniforms sorted
 // (in Fp, as the reference draws them), uploaded; `perm` maps sorted
@@ -678,23 +700,23 @@ template <class T>
 int upload_inputs(qslc_batch *b, const double *angles, const double *u, std::vector<uint32_t> &perm)
 {
     std::vector<T> coef(b->ncoef);
-    uint64_t a = 0;
-    for (uint32_t i = 0; i < b->ninst; i++) {
+    // instance i's angles start at 2 x (its coefficients' offset) / 4
+    host_parallel(b->ninst, [&](uint32_t i) {
         const InstDesc &d = b->inst[i];
+        const double *ai = angles + d.coef / 2;
         for (uint64_t k = 0; k < uint64_t(d.L) * d.n; k++) {
-            const T ry = T(angles[a + 2 * k]), rz = T(angles[a + 2 * k + 1]);
+            const T ry = T(ai[2 * k]), rz = T(ai[2 * k + 1]);
             T *c = &coef[d.coef + 4 * k];
             c[0] = T(std::cos(ry / 2));
             c[1] = T(std::sin(ry / 2));
             c[2] = T(std::cos(rz / 2));
             c[3] = T(std::sin(rz / 2));
         }
-        a += 2 * uint64_t(d.L) * d.n;
-    }
+    });
     const uint32_t ns = b->nshots;
     std::vector<double> us(uint64_t(b->ninst) * ns);
     perm.resize(uint64_t(b->ninst) * ns);
-    for (uint32_t i = 0; i < b->ninst; i++) {
+    host_parallel(b->ninst, [&](uint32_t i) {
         uint32_t *pm = perm.data() + uint64_t(i) * ns;
         const double *ui = u + uint64_t(i) * ns;
         std::iota(pm, pm + ns, 0u);
@@ -704,7 +726,7 @@ int upload_inputs(qslc_batch *b, const double *angles, const double *u, std::vec
             if (b->dtype == QSLC_C64) v = double(float(v));   // the reference draws Fp uniforms
             us[uint64_t(i) * ns + k] = v;
         }
-    }
+    });
     QSLC_CUDA(cudaMemcpyAsync(b->d_coef, coef.data(), coef.size() * sizeof(T), cudaMemcpyHostToDevice, b->stream));
     QSLC_CUDA(cudaMemcpyAsync(b->d_u, us.data(), us.size() * 8, cudaMemcpyHostToDevice, b->stream));
     QSLC_CUDA(cudaStreamSynchronize(b->stream));
@@ -728,9 +750,10 @@ int download(qslc_batch *b, const std::vector<uint32_t> &perm, double *probs, ui
     QSLC_CUDA(cudaGetLastError());
     for (uint64_t i = 0; i < b->nprobs; i++) probs[i] = double(pr[i]);
     const uint32_t ns = b->nshots;
-    for (uint32_t i = 0; i < b->ninst; i++)
+    host_parallel(b->ninst, [&](uint32_t i) {
         for (uint32_t k = 0; k < ns; k++)
             shots[uint64_t(i) * ns + perm[uint64_t(i) * ns + k]] = sh[b->inst[i].shots + k];
+    });
     return QSLC_OK;
 }
 
