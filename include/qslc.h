@@ -276,7 +276,9 @@ QSLC_API int qslc_batch_create(int dtype, uint32_t ninst, const uint32_t *nqubit
 /* angles: per instance, layer-major, per qubit (rotateY angle, rotateZ
  * angle); uniforms: nshots per instance.  probs: per instance 2*n values
  * (prob(q,0), prob(q,1)), q ascending; shots: nshots per instance, in the
- * order of the uniforms. */
+ * order of the uniforms.  The call's host work (coefficients, sorting each
+ * instance's uniforms, reordering the shots) runs on up to 32 host threads
+ * it starts and joins before it returns. */
 QSLC_API int qslc_batch_run(qslc_batch *b, const double *angles, const double *uniforms,
                             double *probs, uint64_t *shots);
 /* Measure every launch shape (threads per CTA, shared-memory tile of 64 or
