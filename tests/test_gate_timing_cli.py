@@ -1,5 +1,7 @@
 """The dense-state gate timer's command line (gate_timing.py, beside
 bench.py): argument checks that need no GPU."""
+import os
+
 import pytest
 
 import gate_timing
@@ -63,3 +65,18 @@ def test_batch_timing_picks_the_bench_instances():
 
 def np_sorted(a):
     return all(a[i] < a[i + 1] for i in range(len(a) - 1))
+
+
+def test_gate_timing_times_single_gates_unless_grouped(monkeypatch):
+    """gate_timing.py switches the library's grouping off (each window then
+    holds one gate's launch) unless --grouped asks for two gates a window."""
+    import gate_timing
+    seen = []
+    monkeypatch.setattr(gate_timing, "run", lambda *a: seen.append((os.environ.get("QSLC_GROUP"), a[-1])))
+    monkeypatch.setenv("QSLC_GROUP", "1")              # restored after the test
+    monkeypatch.delenv("QSLC_GROUP")
+    gate_timing.main(["--gates", "rotateX", "--targets", "1"])
+    assert seen[-1] == ("0", False)
+    monkeypatch.delenv("QSLC_GROUP")
+    gate_timing.main(["--gates", "rotateX", "--targets", "1", "--grouped"])
+    assert seen[-1] == (None, True)
