@@ -173,6 +173,7 @@ int release_held(qslc_state *s)
 int flushed(qslc_state *s)
 {
     int hrc = release_held(s);
+    if (!hrc) hrc = debug_bounds_error();
     if (hrc) return hrc;
     if (!s->fuse_queue.empty()) {
         int rc = fusion_flush(s);

@@ -28,6 +28,28 @@
 namespace qslc {
 namespace {
 
+// Debug builds (-DQSLC_DEBUG_BOUNDS) check each item's largest index
+// against the state's size before the item is read or written: an index
+// outside the state is recorded (the first one) and the item skipped, and
+// the next call that reads the state returns QSLC_EINVAL with the index
+// (debug_bounds_error).  The host validates every qubit index before a
+// launch, so no call through the ABI should record one.  Default builds
+// compile both checks to `true`.
+#ifdef QSLC_DEBUG_BOUNDS
+__device__ unsigned long long g_bad_index;   // first index outside a state, plus one; 0: none
+__device__ __forceinline__ bool in_state(uint64_t i, uint64_t dim)
+{
+    if (i < dim) return true;
+    atomicCAS(&g_bad_index, 0ull, (unsigned long long)i + 1ull);
+    return false;
+}
+#define QSLC_IN_STATE(i, dim) in_state(uint64_t(i), uint64_t(dim))
+#define QSLC_IN_STATE_QUIET(i, dim) (uint64_t(i) < uint64_t(dim))
+#else
+#define QSLC_IN_STATE(i, dim) true
+#define QSLC_IN_STATE_QUIET(i, dim) true
+#endif
+
 
 // One-qubit pair gates: pairs (i0, i0 + 2^t), i0 = insert0(j, t).
 template <class T, int OP, unsigned CPAT = PAT_RUNTIME, class IX = uint64_t>
@@ -43,14 +65,14 @@ __global__ void QSLC_SWEEP_BOUNDS k_pair1(cplx<T> *__restrict__ st, uint64_t npa
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
             i0[r] = ins0<IX>(j + r * stride, t);
-            if (j + r * stride < npairs) {
+            if (j + r * stride < npairs && QSLC_IN_STATE(i0[r] | bit, 2 * npairs)) {
                 a0[r] = st[i0[r]];
                 a1[r] = st[i0[r] | bit];
             }
         }
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
-            if (j + r * stride < npairs) {
+            if (j + r * stride < npairs && QSLC_IN_STATE_QUIET(i0[r] | bit, 2 * npairs)) {
                 pair_update<T, OP>(a0[r], a1[r], k, (pt >> (8 * r)) & 0xFFu);
                 st[i0[r]] = a0[r];
                 st[i0[r] | bit] = a1[r];
@@ -174,11 +196,11 @@ __global__ void QSLC_SWEEP_BOUNDS k_diag1(cplx<T> *__restrict__ st, uint64_t cou
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
             i[r] = ins0<IX>(j + r * stride, t) | bit;
-            if (j + r * stride < count) a[r] = st[i[r]];
+            if (j + r * stride < count && QSLC_IN_STATE(i[r], 2 * count)) a[r] = st[i[r]];
         }
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
-            if (j + r * stride < count) {
+            if (j + r * stride < count && QSLC_IN_STATE_QUIET(i[r], 2 * count)) {
                 diag_update<T, OP>(a[r], k, (pt >> (8 * r)) & 0xFFu);
                 st[i[r]] = a[r];
             }
@@ -269,6 +291,7 @@ __global__ void QSLC_SWEEP_BOUNDS k_group2(cplx<T> *__restrict__ st, uint64_t nq
     const IX stride = IX(gridDim.x) * blockDim.x;
     for (IX j = IX(blockIdx.x) * blockDim.x + threadIdx.x; j < IX(nquads); j += stride) {
         const IX x = ins00<IX>(j, lo, hi);
+        if (!QSLC_IN_STATE(x | c0 | c1, 4 * nquads)) continue;
         cplx<T> a00 = st[x], a01 = st[x | c0], a10 = st[x | c1], a11 = st[x | c0 | c1];
         group_apply<T>(g.op[0], a00, a01, a10, a11, g.k[0]);
         group_apply<T>(g.op[1], a00, a10, a01, a11, g.k[1]);
@@ -301,14 +324,14 @@ __global__ void QSLC_SWEEP_BOUNDS k_pair2(cplx<T> *__restrict__ st, uint64_t nqu
             const IX base = ins00<IX>(j + r * stride, lo, hi);
             x1[r] = base | IX(b1);
             x2[r] = (MODE == 0) ? (x1[r] | IX(b2)) : (base | IX(b2));
-            if (j + r * stride < nquads) {
+            if (j + r * stride < nquads && QSLC_IN_STATE(x1[r] | IX(b2), 4 * nquads)) {
                 a0[r] = st[x1[r]];
                 a1[r] = st[x2[r]];
             }
         }
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
-            if (j + r * stride < nquads) {
+            if (j + r * stride < nquads && QSLC_IN_STATE_QUIET(x1[r] | IX(b2), 4 * nquads)) {
                 pair_update<T, OP>(a0[r], a1[r], k, (pt >> (8 * r)) & 0xFFu);
                 st[x1[r]] = a0[r];
                 st[x2[r]] = a1[r];
@@ -337,11 +360,11 @@ __global__ void QSLC_SWEEP_BOUNDS k_diag2(cplx<T> *__restrict__ st, uint64_t nqu
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
             i[r] = ins00<IX>(j + r * stride, lo, hi) | IX(both);
-            if (j + r * stride < nquads) a[r] = st[i[r]];
+            if (j + r * stride < nquads && QSLC_IN_STATE(i[r], 4 * nquads)) a[r] = st[i[r]];
         }
 #pragma unroll
         for (int r = 0; r < ITEMS; r++) {
-            if (j + r * stride < nquads) {
+            if (j + r * stride < nquads && QSLC_IN_STATE_QUIET(i[r], 4 * nquads)) {
                 diag_update<T, OP>(a[r], k, (pt >> (8 * r)) & 0xFFu);
                 st[i[r]] = a[r];
             }
@@ -880,6 +903,22 @@ bool grouping_enabled()
 int launch_group2(qslc_state *s, const GateOp &g0, const GateOp &g1)
 {
     return s->dtype == QSLC_C128 ? group2_t<double>(s, g0, g1) : group2_t<float>(s, g0, g1);
+}
+
+int debug_bounds_error()
+{
+#ifdef QSLC_DEBUG_BOUNDS
+    unsigned long long bad = 0;
+    QSLC_CUDA(cudaDeviceSynchronize());
+    QSLC_CUDA(cudaMemcpyFromSymbol(&bad, g_bad_index, sizeof(bad)));
+    if (bad) {
+        const unsigned long long zero = 0;
+        QSLC_CUDA(cudaMemcpyToSymbol(g_bad_index, &zero, sizeof(zero)));
+        return fail(QSLC_EINVAL, "a sweep indexed outside the state (debug bounds check): index " +
+                                     std::to_string(bad - 1));
+    }
+#endif
+    return QSLC_OK;
 }
 
 int launch_gate1(qslc_state *s, int gate, unsigned targ, double angle)

@@ -177,6 +177,10 @@ int launch_gate2(qslc_state *s, int gate, unsigned q1, unsigned q2, double angle
 // two one-qubit gates on different qubits, in this order, in one sweep
 int launch_group2(qslc_state *s, const GateOp &g0, const GateOp &g1);
 bool grouping_enabled();
+// Debug builds (-DQSLC_DEBUG_BOUNDS): QSLC_EINVAL when a sweep met an index
+// outside its state since the last call; QSLC_OK otherwise and in default
+// builds.
+int debug_bounds_error();
 int launch_collapse(qslc_state *s, unsigned targ, unsigned outcome, double factor);
 // complex64 collapse with the factor applied in double (precision form)
 int launch_collapse_f64(qslc_state *s, unsigned targ, unsigned outcome, double factor);
